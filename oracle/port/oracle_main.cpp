@@ -1,0 +1,131 @@
+// Command-line front end of the oracle restatement: the reference's find-clumps command
+// line (src/global.cpp:247-289) over the CPU restatement. Test infrastructure only.
+#include "oracle.hpp"
+
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <getopt.h>
+#include <iomanip>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+using namespace orc;
+
+static double now() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+int main(int argc, char **argv) {
+    static int f_combined = 0, f_find = 0, f_save = 0, f_noghost = 0, f_basic = 0, f_dvs = 0, f_tmp = 0, f_help = 0, f_dbg = 0, f_verb = 0;
+    static struct option opts[] = {
+        {"Debug", no_argument, &f_dbg, 1},         {"Verbose", no_argument, &f_verb, 1},
+        {"Combined", no_argument, &f_combined, 1}, {"Find_Clumps", no_argument, &f_find, 1},
+        {"Save_Clumps", no_argument, &f_save, 1},  {"No_Ghost", no_argument, &f_noghost, 1},
+        {"Basic_Analyses", no_argument, &f_basic, 1}, {"Density_Vs_Scale", no_argument, &f_dvs, 1},
+        {"Temp_Calculation", no_argument, &f_tmp, 1}, {"Help", no_argument, &f_help, 1},
+        {"num_cpus", required_argument, nullptr, 'c'}, {"data_dir", required_argument, nullptr, 'i'},
+        {"basename", required_argument, nullptr, 'b'}, {"postname", required_argument, nullptr, 'p'},
+        {"file_num", required_argument, nullptr, 'f'}, {"out_file", required_argument, nullptr, 'o'},
+        {"in_const", required_argument, nullptr, 't'}, {"sampling", required_argument, nullptr, 's'},
+        {"xlim", required_argument, nullptr, 'x'}, {"ylim", required_argument, nullptr, 'y'},
+        {"zlim", required_argument, nullptr, 'z'}, {"pow_mode", required_argument, nullptr, 'P'},
+        {"threads", required_argument, nullptr, 'T'}, {nullptr, 0, nullptr, 0}};
+    int num_cpus = 1, start = 0, end = 0, step = 1, pow_mode = 0, threads = 0;
+    unsigned sampling = 1;
+    std::string dir, base, post, out, param;
+    int o, idx;
+    while ((o = getopt_long(argc, argv, ":c:i:b:p:f:o:t:s:x:y:z:hP:T:", opts, &idx)) != -1) {
+        switch (o) {
+        case 0: break;
+        case 'c': num_cpus = std::atoi(optarg); break;
+        case 'i': dir = optarg; break;
+        case 'b': base = optarg; break;
+        case 'p': post = optarg; break;
+        case 'f': {
+            std::string s(optarg);
+            char ch;
+            if (s.find_first_of(':') == s.find_last_of(':')) {
+                std::istringstream is(s);
+                is >> start >> ch >> end;
+            } else {
+                std::istringstream is(s.substr(0, s.find_last_of(':')));
+                is >> start >> ch >> end;
+                step = std::atoi(s.substr(s.find_last_of(':') + 1).c_str());
+            }
+            if (start < 0) start = 0;
+            if (end < start) end = start;
+            if (step == 0) step = 1;
+            break;
+        }
+        case 'o': out = optarg; break;
+        case 't': param = optarg; break;
+        case 's': sampling = (unsigned)std::atoi(optarg); if (sampling == 0) sampling = 1; break;
+        case 'P': pow_mode = std::atoi(optarg); break;
+        case 'T': threads = std::atoi(optarg); break;
+        case 'h': f_help = 1; break;
+        case 'x': case 'y': case 'z': break;  // user box: not used by the oracle's tests
+        default: std::fprintf(stderr, "Error: Unknown/invalid option\n"); return 2;
+        }
+    }
+    if (f_help || out.empty()) { std::fprintf(stderr, "usage: oracle_plan -c N -i dir -b base -p post -f a:b[:s] -o out -t params [--Combined]\n"); return 0; }
+    if (!dir.empty() && dir.back() != '/') dir.push_back('/');
+    Params par;
+    if (!param.empty()) { int rc = read_param_file(param, par); if (rc) return rc; }
+    int nthreads = threads > 0 ? threads : (int)par.num_threads;
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#endif
+    if (nthreads <= 0) nthreads = 1;
+    bool first = true;
+    std::string stem = out.substr(0, out.find_last_of('.')) + "_planetesimals.txt";
+    FILE *pf = std::fopen(stem.c_str(), "w");
+    if (!pf) return 3;
+    for (int num = start; num <= end; num += step) {
+        std::ostringstream nn;
+        nn << std::setw(4) << std::setfill('0') << num;
+        std::vector<std::string> files;
+        if (f_combined) {
+            files.push_back(dir + base + "." + nn.str() + "." + post + ".lis");
+        } else {
+            files.push_back(dir + "id0/" + base + "." + nn.str() + "." + post + ".lis");
+            for (int id = 1; id < num_cpus; ++id)
+                files.push_back(dir + "id" + std::to_string(id) + "/" + base + "-id" + std::to_string(id) + "." + nn.str() + "." + post + ".lis");
+        }
+        double t0 = now();
+        Snapshot snap;
+        int rc = read_lis_files(files, snap);
+        if (rc) return rc;
+        finish_read(snap, par, first);
+        uint32_t nin = snap.num_particles;
+        double t1 = now();
+        if (!f_noghost) make_ghosts(snap, par);
+        Finder f;
+        f.par = &par;
+        f.threads = nthreads;
+        f.pow_mode = pow_mode ? POW_CORRECT : POW_LIBM;
+        f.time = snap.time;
+        f.tree.build(par, snap.parts, true);
+        double t2 = now();
+        std::string summary = f.find(nin);
+        double t3 = now();
+        std::printf("%s\n", summary.c_str());
+        write_peaks_file(peaks_file_name(out, snap.time), f);
+        if (f_save) {
+            std::ostringstream sid;
+            sid << std::setw(4) << std::setfill('0') << num;
+            write_parlists("ParList." + sid.str(), f, sampling);
+        }
+        std::string line = (first ? basic_results_header() : std::string()) + basic_results_line(f, par, snap.time);
+        std::fwrite(line.data(), 1, line.size(), pf);
+        std::fprintf(stderr, "[oracle] read %.4f s, ghost+tree %.4f s, find %.4f s, tree points %u, threads %d\n", t1 - t0, t2 - t1, t3 - t2, f.tree.size(), nthreads);
+        first = false;
+    }
+    std::fclose(pf);
+    return 0;
+}
