@@ -1,0 +1,253 @@
+// C entry points (include/plan_gpu.h): context management, the BuildTree and
+// FindPlanetesimals seams, and inspection of stage arrays.
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "catalogue.h"
+#include "hop.h"
+#include "pipeline.h"
+
+namespace plan {
+
+thread_local Context *g_ctx = nullptr;
+
+int set_cuda_error(cudaError_t e, const char *what, const char *file, int line) {
+    if (g_ctx) {
+        char buf[512];
+        std::snprintf(buf, sizeof(buf), "CUDA error %s (%s) at %s:%d: %s", cudaGetErrorName(e), cudaGetErrorString(e), file, line, what);
+        g_ctx->last_error = buf;
+    }
+    if (e == cudaErrorMemoryAllocation) return kErrOutOfMemory;
+    return kErrDevice;
+}
+
+int Context::status_from(int rc, const char *what) {
+    if (rc != kOk && last_error.empty()) last_error = std::string(what) + ": status " + std::to_string(rc);
+    return rc;
+}
+
+int Context::ensure(Arena &a, size_t bytes) {
+    if (a.cap >= bytes) return kOk;
+    if (a.base) cudaFree(a.base);
+    a.base = nullptr;
+    a.cap = 0;
+    a.used = 0;
+    size_t want = bytes + bytes / 16 + (64u << 20);
+    cudaError_t e = cudaMalloc(&a.base, want);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        last_error = "device allocation of " + std::to_string(want >> 20) + " MiB failed";
+        return kErrOutOfMemory;
+    }
+    a.cap = want;
+    return kOk;
+}
+
+// Device bytes for a snapshot of n input particles with the ghost count of a uniform box
+// (T = 1.5625 n); the exact count is known, and the arena grown to it, during the build.
+static void footprint(uint64_t n, uint64_t &arena, uint64_t &scratch) {
+    uint64_t T = n + n * 9 / 16 + 1024;
+    arena = T * kArenaBytesPerTreePoint + (64ull << 20);
+    scratch = (4 * n + 1024) * 40 > n * kScratchBytesPerParticle ? (4 * n + 1024) * 40 : n * kScratchBytesPerParticle;
+    scratch += 64ull << 20;
+}
+
+}  // namespace plan
+
+using namespace plan;
+
+struct plan_ctx {
+    Context c;
+};
+
+extern "C" {
+
+int plan_ctx_create(int device, plan_ctx **out) {
+    if (!out) return kErrArgument;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0 || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return kErrDevice;
+    }
+    plan_ctx *h = new plan_ctx();
+    Context &c = h->c;
+    g_ctx = &c;
+    c.device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&c.d_err, 16) != cudaSuccess || cudaMemset(c.d_err, 0, 16) != cudaSuccess) {
+        delete h;
+        return kErrDevice;
+    }
+    *out = h;
+    return kOk;
+}
+
+void plan_ctx_destroy(plan_ctx *h) {
+    if (!h) return;
+    Context &c = h->c;
+    cudaSetDevice(c.device);
+    if (c.stream) cudaStreamSynchronize(c.stream);
+    if (c.arena.base) cudaFree(c.arena.base);
+    if (c.scratch.base) cudaFree(c.scratch.base);
+    if (c.d_err) cudaFree(c.d_err);
+    if (c.stream) cudaStreamDestroy(c.stream);
+    if (g_ctx == &c) g_ctx = nullptr;
+    delete h;
+}
+
+const char *plan_last_error(const plan_ctx *h) { return h ? h->c.last_error.c_str() : "no context"; }
+
+uint64_t plan_footprint_bytes(uint64_t n, const plan_params *) {
+    uint64_t a, s;
+    footprint(n, a, s);
+    return a + s;
+}
+
+int plan_build_tree(plan_ctx *h, const plan_lis_view *v, plan_params *p, int first_file, void *stream) {
+    if (!h || !v || !p) return kErrArgument;
+    Context &c = h->c;
+    g_ctx = &c;
+    c.last_error.clear();
+    cudaSetDevice(c.device);
+    uint64_t n = 0;
+    for (uint32_t b = 0; b < v->nblocks; ++b) n += v->counts[b];
+    uint64_t need_a, need_s;
+    footprint(n, need_a, need_s);
+    if (c.ensure(c.scratch, need_s)) return c.status_from(kErrOutOfMemory, "plan_build_tree");
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c.stream;
+    cudaMemsetAsync(c.d_err, 0, 16, s);
+    int rc = build_tree(c, *v, *p, first_file, s);
+    if (rc == kOk) {
+        unsigned err = 0;
+        cudaMemcpy(&err, c.d_err, 4, cudaMemcpyDeviceToHost);
+        c.counters[9] = err;
+        if (err) {
+            c.last_error = "device error flags " + std::to_string(err) + " while building the tree";
+            rc = kErrDeviceLimit;
+        }
+    }
+    return c.status_from(rc, "plan_build_tree");
+}
+
+int plan_find_planetesimals(plan_ctx *h, plan_params *p, void *stream, plan_catalogue **out) {
+    if (!h || !p) return kErrArgument;
+    Context &c = h->c;
+    g_ctx = &c;
+    c.last_error.clear();
+    cudaSetDevice(c.device);
+    if (!c.tree.Tu) return kErrArgument;
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c.stream;
+    int rc = find_planetesimals(c, *p, s, out);
+    unsigned err = 0;
+    cudaMemcpy(&err, c.d_err, 4, cudaMemcpyDeviceToHost);
+    c.counters[9] = err;
+    if (rc == kOk && err) {
+        c.last_error = "device error flags " + std::to_string(err) + " while finding clumps";
+        rc = kErrDeviceLimit;
+    }
+    return c.status_from(rc, "plan_find_planetesimals");
+}
+
+int plan_find_clumps(plan_ctx *h, const plan_lis_view *v, plan_params *p, int first_file, void *stream, plan_catalogue **out) {
+    int rc = plan_build_tree(h, v, p, first_file, stream);
+    if (rc) return rc;
+    return plan_find_planetesimals(h, p, stream, out);
+}
+
+uint64_t plan_stage_count(const plan_ctx *h, int which) {
+    if (!h) return 0;
+    const DevTree &t = h->c.tree;
+    switch (which) {
+    case PLAN_ARR_TREE_POS: case PLAN_ARR_TREE_VEL: case PLAN_ARR_DENSITY: case PLAN_ARR_ORIG_ID: case PLAN_ARR_KEYS:
+    case PLAN_ARR_SINK_COUNT:
+        return t.Tu;
+    case PLAN_ARR_NODE_F: case PLAN_ARR_NODE_U:
+        return t.nodes;
+    case PLAN_ARR_DENSEST: case PLAN_ARR_PEAK:
+        return h->c.densest ? t.Tu : 0;
+    default:
+        return 0;
+    }
+}
+
+int plan_stage_copy(plan_ctx *h, int which, void *dst, size_t bytes) {
+    if (!h || !dst) return kErrArgument;
+    Context &c = h->c;
+    g_ctx = &c;
+    cudaSetDevice(c.device);
+    const DevTree &t = c.tree;
+    size_t n = plan_stage_count(h, which);
+    if (!n) return kErrArgument;
+    auto copy = [&](const void *src, size_t b) -> int {
+        if (bytes < b) return kErrArgument;
+        PLAN_CUDA(cudaMemcpy(dst, src, b, cudaMemcpyDeviceToHost));
+        return kOk;
+    };
+    switch (which) {
+    case PLAN_ARR_TREE_POS: return copy(t.pos, n * 32);
+    case PLAN_ARR_TREE_VEL: return copy(t.vel, n * 32);
+    case PLAN_ARR_DENSITY: return copy(t.dens, n * 8);
+    case PLAN_ARR_ORIG_ID: return copy(t.orig, n * 4);
+    case PLAN_ARR_SINK_COUNT: return copy(t.sink_n, n * 4);
+    case PLAN_ARR_DENSEST: return copy(c.densest, n * 4);
+    case PLAN_ARR_PEAK: return copy(c.peak, n * 4);
+    case PLAN_ARR_KEYS: {
+        if (bytes < n * 12) return kErrArgument;
+        std::vector<uint32_t> a(n), b(n), d(n);
+        PLAN_CUDA(cudaMemcpy(a.data(), t.tk0, n * 4, cudaMemcpyDeviceToHost));
+        PLAN_CUDA(cudaMemcpy(b.data(), t.tk1, n * 4, cudaMemcpyDeviceToHost));
+        PLAN_CUDA(cudaMemcpy(d.data(), t.tk2, n * 4, cudaMemcpyDeviceToHost));
+        uint32_t *o = static_cast<uint32_t *>(dst);
+        for (size_t i = 0; i < n; ++i) { o[3 * i] = a[i]; o[3 * i + 1] = b[i]; o[3 * i + 2] = d[i]; }
+        return kOk;
+    }
+    case PLAN_ARR_NODE_F: return copy(t.ncf, n * 32);
+    case PLAN_ARR_NODE_U: {
+        if (bytes < n * 28) return kErrArgument;
+        std::vector<uint32_t> b(n), e(n), p(n), fd(n), nd(n);
+        std::vector<uint8_t> o(n), l(n);
+        PLAN_CUDA(cudaMemcpy(b.data(), t.nbeg, n * 4, cudaMemcpyDeviceToHost));
+        PLAN_CUDA(cudaMemcpy(e.data(), t.nend, n * 4, cudaMemcpyDeviceToHost));
+        PLAN_CUDA(cudaMemcpy(p.data(), t.npar, n * 4, cudaMemcpyDeviceToHost));
+        PLAN_CUDA(cudaMemcpy(fd.data(), t.nfd, n * 4, cudaMemcpyDeviceToHost));
+        PLAN_CUDA(cudaMemcpy(nd.data(), t.nnd, n * 4, cudaMemcpyDeviceToHost));
+        PLAN_CUDA(cudaMemcpy(o.data(), t.north, n, cudaMemcpyDeviceToHost));
+        PLAN_CUDA(cudaMemcpy(l.data(), t.nlev, n, cudaMemcpyDeviceToHost));
+        uint32_t *u = static_cast<uint32_t *>(dst);
+        for (size_t i = 0; i < n; ++i) {
+            u[7 * i] = b[i]; u[7 * i + 1] = e[i]; u[7 * i + 2] = p[i]; u[7 * i + 3] = fd[i];
+            u[7 * i + 4] = o[i]; u[7 * i + 5] = nd[i]; u[7 * i + 6] = l[i];
+        }
+        return kOk;
+    }
+    default:
+        return kErrArgument;
+    }
+}
+
+int plan_knn(plan_ctx *h, const double *pos3, uint32_t nq, uint32_t k, double est, uint32_t *idx, double *dr2) {
+    if (!h || !pos3 || !idx || !dr2) return kErrArgument;
+    Context &c = h->c;
+    g_ctx = &c;
+    cudaSetDevice(c.device);
+    return c.status_from(knn_positions(c, pos3, nq, k, est, idx, dr2), "plan_knn");
+}
+
+int plan_stage_times(const plan_ctx *h, double *ms, int n) {
+    if (!h || !ms) return kErrArgument;
+    for (int i = 0; i < n && i < 16; ++i) ms[i] = h->c.stage_ms[i];
+    return kOk;
+}
+
+uint64_t plan_kernel_launches(const plan_ctx *h) { return h ? h->c.launches : 0; }
+
+int plan_counters(const plan_ctx *h, uint64_t *out, int n) {
+    if (!h || !out) return kErrArgument;
+    for (int i = 0; i < n && i < 16; ++i) out[i] = h->c.counters[i];
+    return kOk;
+}
+
+}  // extern "C"

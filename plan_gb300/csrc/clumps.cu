@@ -1,0 +1,1487 @@
+// FindPlanetesimals on the device (src/tree.hpp:3576-4339) and the per-clump operations of
+// Planetesimal / PlanetesimalList (src/tree.hpp:4351-4909, 5251-5284).
+//
+// Clumps live in a slot table (structure of arrays). Members live in a pool: each clump
+// owns one contiguous segment holding its `indices` order together with the distances of
+// its `particles` list (the reference keeps both vectors in the same order outside the
+// short windows in which it permutes them). Segments are bump-allocated; merging or
+// growing a clump writes a new segment.
+//
+// Sequential semantics are kept where the reference has them:
+//  * sums run in member order on one thread (kinematics, dispersion, two-sigma mass, J);
+//  * merge sweeps evaluate every candidate pair in parallel (ball search over a clump tree,
+//    boundness, saddle densities by KNN), then one thread resolves predator/prey in key
+//    order; predators merge in waves so a predator that is itself eaten later is complete
+//    first (the serial order of src/tree.hpp:3976-3980);
+//  * unbinding scans members from the outermost inwards with the current state; a chunk of
+//    candidates is evaluated in parallel and the highest-index unbound member is removed
+//    before the rest is re-evaluated (exact, since only removals change the state);
+//  * Hill-sphere rebinding runs clump by clump in key order (the in-clump flags couple
+//    clumps); inside a clump the first bound candidate of each chunk is accepted the same way.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <numeric>
+#include <vector>
+
+#include "catalogue.h"
+#include "hop.h"
+#include "pipeline.h"
+#include "sort.h"
+#include "tree_walk.cuh"
+
+namespace plan {
+
+namespace {
+
+constexpr uint32_t kNone = 0xffffffffu;
+constexpr int kSmallSort = 2048;
+
+struct CP {
+    double G, shear, Omega;
+    double thr, peak_thr, mass_thr;
+    double diffuse, hillf;
+    uint32_t knn, Tu;
+};
+
+struct CT {  // clump table
+    uint32_t C;
+    uint32_t *key, *peak;
+    uint8_t *mask, *alive;
+    double *M;
+    double4_32a *com, *vcom, *J;
+    double *r_in, *r_out, *r10, *r2s, *hill;
+    uint32_t *moff, *mn;
+    uint32_t *sub_head, *sub_tail;
+};
+
+struct Pool {
+    uint32_t *idx;
+    double *dist;
+    uint32_t *top;
+    uint32_t cap;
+    uint32_t *sub_peak, *sub_next, *sub_top;
+    uint32_t sub_cap;
+};
+
+__device__ __forceinline__ double norm3(double x, double y, double z) {
+    double s = x * x;
+    s = s + y * y;
+    s = s + z * z;
+    return sqrt(s);
+}
+
+__device__ __forceinline__ double norm2_3(double x, double y, double z) {
+    double s = x * x;
+    s = s + y * y;
+    s = s + z * z;
+    return s;
+}
+
+__device__ uint32_t pool_alloc(const Pool &P, uint32_t n, unsigned *err) {
+    uint32_t o = atomicAdd(P.top, n);
+    if (o + n > P.cap || o + n < o) {
+        atomicOr(err, (unsigned)kDevErrCapacity);
+        return kNone;
+    }
+    return o;
+}
+
+// ---------------------------------------------------------------- setup
+__global__ void k_init(uint32_t C, const uint32_t *gkey, const uint32_t *goff, CT ct, uint32_t *slot_of_key) {
+    uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= C) return;
+    uint32_t k = gkey[g];
+    ct.key[g] = k;
+    ct.peak[g] = k;
+    ct.mask[g] = 1;
+    ct.alive[g] = 1;
+    ct.moff[g] = goff[g];
+    ct.mn[g] = goff[g + 1] - goff[g];
+    ct.sub_head[g] = kNone;
+    ct.sub_tail[g] = kNone;
+    ct.hill[g] = 0;
+    ct.J[g] = make_double4_32a(0, 0, 0, 0);
+    slot_of_key[k] = g;
+}
+
+// CalculateKinematicProperties (src/tree.hpp:4431-4442): one thread per clump, in order.
+__global__ void k_kinematics(const uint32_t *list, uint32_t n, CT ct, Pool P, const double4_32a *pos, const double4_32a *vel) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    uint32_t s = list[t];
+    double M = 0, cx = 0, cy = 0, cz = 0, vx = 0, vy = 0, vz = 0;
+    const uint32_t o = ct.moff[s], m = ct.mn[s];
+    for (uint32_t k = 0; k < m; ++k) {
+        uint32_t i = P.idx[o + k];
+        double4_32a p = pos[i], v = vel[i];
+        M = M + p.w;
+        cx = cx + p.x * p.w; cy = cy + p.y * p.w; cz = cz + p.z * p.w;
+        vx = vx + v.x * p.w; vy = vy + v.y * p.w; vz = vz + v.z * p.w;
+    }
+    ct.M[s] = M;
+    ct.com[s] = make_double4_32a(cx / M, cy / M, cz / M, 0);
+    ct.vcom[s] = make_double4_32a(vx / M, vy / M, vz / M, 0);
+}
+
+// distances to the centre of mass (src/tree.hpp:4448-4450, 4545-4547)
+__global__ void k_dist(const uint32_t *list, CT ct, Pool P, const double4_32a *pos) {
+    uint32_t s = list[blockIdx.x];
+    const uint32_t o = ct.moff[s], m = ct.mn[s];
+    double4_32a c = ct.com[s];
+    for (uint32_t k = threadIdx.x; k < m; k += blockDim.x) {
+        double4_32a p = pos[P.idx[o + k]];
+        P.dist[o + k] = norm3(p.x - c.x, p.y - c.y, p.z - c.z);
+    }
+}
+
+// in-block bitonic sort by (distance, previous position) for segments <= kSmallSort
+__global__ void __launch_bounds__(1024) k_sort_small(const uint32_t *list, CT ct, Pool P) {
+    __shared__ unsigned long long sk[kSmallSort];
+    __shared__ uint32_t si[kSmallSort];
+    __shared__ uint16_t sp[kSmallSort];
+    uint32_t s = list[blockIdx.x];
+    const uint32_t o = ct.moff[s], m = ct.mn[s];
+    if (m > kSmallSort || m < 2) return;
+    uint32_t n2 = 1;
+    while (n2 < m) n2 <<= 1;
+    for (uint32_t k = threadIdx.x; k < n2; k += blockDim.x) {
+        if (k < m) {
+            sk[k] = (unsigned long long)__double_as_longlong(P.dist[o + k]);
+            si[k] = P.idx[o + k];
+            sp[k] = (uint16_t)k;
+        } else {
+            sk[k] = ~0ull;
+            si[k] = kNone;
+            sp[k] = 0xffff;
+        }
+    }
+    __syncthreads();
+    for (uint32_t size = 2; size <= n2; size <<= 1) {
+        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+            for (uint32_t k = threadIdx.x; k < n2; k += blockDim.x) {
+                uint32_t j = k ^ stride;
+                if (j > k) {
+                    bool up = (k & size) == 0;
+                    bool gt = sk[k] > sk[j] || (sk[k] == sk[j] && sp[k] > sp[j]);
+                    if (gt == up) {
+                        unsigned long long tk = sk[k]; sk[k] = sk[j]; sk[j] = tk;
+                        uint32_t ti = si[k]; si[k] = si[j]; si[j] = ti;
+                        uint16_t tp = sp[k]; sp[k] = sp[j]; sp[j] = tp;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (uint32_t k = threadIdx.x; k < m; k += blockDim.x) {
+        P.idx[o + k] = si[k];
+        P.dist[o + k] = __longlong_as_double((long long)sk[k]);
+    }
+}
+
+// radii after a sort (src/tree.hpp:4461-4511)
+__global__ void k_one10th(const uint32_t *list, CT ct, Pool P, const double4_32a *pos, const double *dens) {
+    __shared__ uint32_t s_in, s_out;
+    uint32_t s = list[blockIdx.x];
+    const uint32_t o = ct.moff[s], m = ct.mn[s];
+    if (m == 0) return;
+    if (threadIdx.x == 0) { s_in = kNone; s_out = 0; }
+    __syncthreads();
+    const double tenth = dens[P.idx[o + m / 2]] / 10.;
+    for (uint32_t k = threadIdx.x; k < m; k += blockDim.x) {
+        double d = dens[P.idx[o + k]];
+        if (d < tenth) atomicMin(&s_in, k);       // first member below a tenth of the median's density
+        if (d > tenth) atomicMax(&s_out, k + 1);  // last member above it (stored +1)
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    double rin = (s_in != kNone) ? P.dist[o + s_in] : P.dist[o + m - 1];
+    double rout = P.dist[o + (s_out ? s_out - 1 : 0)];
+    double r10 = (rin + rout) / 2.;
+    double tm = 0., tenth_mass = ct.M[s] * (1.0 - 0.95);
+    uint32_t r = m;
+    for (; r > 0; --r) {
+        tm = tm + pos[P.idx[o + r - 1]].w;
+        if (tm > tenth_mass) break;
+    }
+    double r2s = P.dist[o + (r ? r - 1 : 0)];
+    if (rin > 0 && rout / rin > 2.5) r10 = (r2s < rout) ? r2s : rout;
+    else r10 = (r2s < r10) ? r2s : r10;
+    ct.r_in[s] = rin;
+    ct.r_out[s] = rout;
+    ct.r10[s] = r10;
+    ct.r2s[s] = r2s;
+}
+
+// IsPositionDispersion2Large (src/tree.hpp:4516-4528): sequential sum of squares
+__global__ void k_dispersion(const uint32_t *list, uint32_t n, CT ct, Pool P, double tol, uint8_t *too_large) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    uint32_t s = list[t];
+    const uint32_t o = ct.moff[s], m = ct.mn[s];
+    if (m == 0) { too_large[t] = 0; return; }
+    double acc = 0.0;
+    for (uint32_t k = 0; k < m; ++k) acc = acc + P.dist[o + k] * P.dist[o + k];
+    double x = tol * P.dist[o + m - 1];
+    too_large[t] = (acc / (double)m > x * x) ? 1 : 0;
+}
+
+__global__ void k_hill(const uint32_t *list, uint32_t n, CT ct, double G, double Omega) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    uint32_t s = list[t];
+    ct.hill[s] = cr_pow_third(ct.M[s] * G / 3. / Omega / Omega);  // src/tree.hpp:4715-4717
+}
+
+// ---------------------------------------------------------------- large segment sort
+__global__ void k_large_gather(const uint32_t *list, uint32_t nl, const uint32_t *base, CT ct, Pool P, uint32_t *w0, uint32_t *w1,
+                               uint32_t *w2, uint32_t *pay) {
+    uint32_t t = blockIdx.x;
+    if (t >= nl) return;
+    uint32_t s = list[t];
+    const uint32_t o = ct.moff[s], m = ct.mn[s], b = base[t];
+    for (uint32_t k = threadIdx.x; k < m; k += blockDim.x) {
+        unsigned long long bits = (unsigned long long)__double_as_longlong(P.dist[o + k]);
+        w0[b + k] = (uint32_t)bits;
+        w1[b + k] = (uint32_t)(bits >> 32);
+        w2[b + k] = t;
+        pay[b + k] = P.idx[o + k];
+    }
+}
+
+__global__ void k_large_scatter(const uint32_t *list, uint32_t nl, const uint32_t *base, CT ct, Pool P, const uint32_t *w0,
+                                const uint32_t *w1, const uint32_t *pay) {
+    uint32_t t = blockIdx.x;
+    if (t >= nl) return;
+    uint32_t s = list[t];
+    const uint32_t o = ct.moff[s], m = ct.mn[s], b = base[t];
+    for (uint32_t k = threadIdx.x; k < m; k += blockDim.x) {
+        unsigned long long bits = ((unsigned long long)w1[b + k] << 32) | w0[b + k];
+        P.dist[o + k] = __longlong_as_double((long long)bits);
+        P.idx[o + k] = pay[b + k];
+    }
+}
+
+// ---------------------------------------------------------------- merge sweeps
+__global__ void k_mark_live(uint32_t C, CT ct, uint32_t *flag) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= C) return;
+    flag[s] = (ct.alive[s] && ct.mask[s]) ? 1u : 0u;
+}
+
+__global__ void k_ct_points(uint32_t C, CT ct, const uint32_t *flag, const uint32_t *rank, double mass0, double4_32a *pos, double4_32a *vel,
+                            uint32_t *ct_slot) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= C || !flag[s]) return;
+    uint32_t k = rank[s];
+    double4_32a c = ct.com[s], v = ct.vcom[s];
+    pos[k] = make_double4_32a(c.x, c.y, c.z, mass0);
+    vel[k] = make_double4_32a(v.x, v.y, v.z, (double)ct.key[s]);  // the clump tree's density field holds the key
+    ct_slot[k] = s;
+}
+
+__device__ __forceinline__ double merge_radius(const CT &ct, uint32_t s, bool hill_mode, double hillf) {
+    return hill_mode ? ct.hill[s] * hillf : ct.r10[s];
+}
+
+__global__ void k_max_radius(uint32_t C, CT ct, bool hill_mode, double hillf, double *out) {
+    __shared__ double sm[1024];
+    double m = 0;
+    for (uint32_t s = threadIdx.x; s < C; s += blockDim.x)
+        if (ct.alive[s] && ct.mask[s]) { double r = merge_radius(ct, s, hill_mode, hillf); m = (m < r) ? r : m; }
+    sm[threadIdx.x] = m;
+    __syncthreads();
+    for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+        if ((int)threadIdx.x < st) sm[threadIdx.x] = fmax(sm[threadIdx.x], sm[threadIdx.x + st]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = sm[0];
+}
+
+// BallSearch on the clump tree for every live clump (src/tree.hpp:3898, 4043); pass 0
+// counts, pass 1 fills candidate clump-tree indices in traversal order.
+__global__ void k_ball_clumps(int pass, uint32_t C, CT ct, KTree t, bool hill_mode, double hillf, double max_radius, uint32_t *cnt,
+                              const uint32_t *off, uint32_t *cand, unsigned *err) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= C) return;
+    if (!(ct.alive[s] && ct.mask[s])) {
+        if (pass == 0) cnt[s] = 0;
+        return;
+    }
+    double4_32a c = ct.com[s];
+    double r = merge_radius(ct, s, hill_mode, hillf) + max_radius;
+    double r2 = r * r;
+    uint32_t n = 0, o = pass ? off[s] : 0;
+    traverse(t, c.x, c.y, c.z, r,
+             [&](uint32_t b, uint32_t e, bool partial) {
+                 for (uint32_t q = b; q < e; ++q) {
+                     if (partial && !(point_dr2(c.x, c.y, c.z, t.pos[q]) <= r2)) continue;
+                     if (pass) cand[o + n] = q;
+                     ++n;
+                 }
+                 return true;
+             },
+             err);
+    if (pass == 0) cnt[s] = n;
+}
+
+// Per candidate pair: contained, or intersecting and bound (then the saddle decides).
+// code: 0 no, 1 eat, 2 needs saddle test, 3 self, 4 unknown key
+__global__ void k_pair_eval(uint32_t ncand, const uint32_t *cand_p1, const uint32_t *cand, const double4_32a *ctvel, CT ct,
+                            const uint32_t *slot_of_key, CP cp, bool hill_mode, uint8_t *code, uint32_t *p2_of, double *sq, double *sest,
+                            uint32_t *saddle_of, uint32_t *nsaddle) {
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= ncand) return;
+    uint32_t p1 = cand_p1[k];
+    uint32_t key2 = (uint32_t)ctvel[cand[k]].w;
+    p2_of[k] = kNone;
+    if (key2 == ct.key[p1]) { code[k] = 3; return; }
+    uint32_t p2 = key2 < cp.Tu ? slot_of_key[key2] : kNone;
+    if (p2 == kNone) { code[k] = 4; return; }
+    p2_of[k] = p2;
+    double r1 = merge_radius(ct, p1, hill_mode, cp.hillf), r2 = merge_radius(ct, p2, hill_mode, cp.hillf);
+    double4_32a c1 = ct.com[p1], c2 = ct.com[p2];
+    double dist = norm3(c1.x - c2.x, c1.y - c2.y, c1.z - c2.z);
+    uint8_t out = 0;
+    if (dist < fmax(r1, r2)) {
+        out = 1;
+    } else if (dist < (r1 + r2)) {
+        // IsGravitationallyBound (src/tree.hpp:4867-4874)
+        double M = ct.M[p1] + ct.M[p2];
+        double pg = -cp.G / norm3(c1.x - c2.x, c1.y - c2.y, c1.z - c2.z);
+        double4_32a v1 = ct.vcom[p1], v2 = ct.vcom[p2];
+        double dx = c1.x - c2.x;
+        double ex = (v1.x - 0.0 * dx) - v2.x, ey = (v1.y - cp.shear * dx) - v2.y, ez = (v1.z - 0.0 * dx) - v2.z;
+        double ek = 0.5 / M * norm2_3(ex, ey, ez);
+        if (pg + ek < 0.) {
+            // saddle point between the two (src/tree.hpp:4880-4909)
+            double ra = hill_mode ? ct.hill[p1] : ct.r10[p1], rb = hill_mode ? ct.hill[p2] : ct.r10[p2];
+            double f = ra / (ra + rb);
+            uint32_t q = atomicAdd(nsaddle, 1u);
+            sq[3 * q] = c1.x + (c2.x - c1.x) * f;
+            sq[3 * q + 1] = c1.y + (c2.y - c1.y) * f;
+            sq[3 * q + 2] = c1.z + (c2.z - c1.z) * f;
+            double est = fmin(ra, rb);
+            sest[q] = hill_mode ? est / cp.hillf : est;
+            saddle_of[q] = k;
+            out = 2;
+        }
+    }
+    code[k] = out;
+}
+
+__global__ void k_saddle_apply(uint32_t ns, const uint32_t *saddle_of, const double *sdens, double limit, uint8_t *code) {
+    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= ns) return;
+    // merge when the saddle is NOT deep: density >= 2.5 rho_thr
+    code[saddle_of[q]] = (sdens[q] < limit) ? 0 : 1;
+}
+
+// Serial predator/prey resolution in key order (src/tree.hpp:3894-3951), one thread.
+__global__ void k_resolve(uint32_t C, CT ct, const uint32_t *cnt, const uint32_t *off, const uint8_t *code, const uint32_t *p2_of,
+                          uint32_t *pairs, uint32_t *npairs, uint32_t *del_keys, uint32_t *ndel, uint32_t *nunknown) {
+    if (threadIdx.x || blockIdx.x) return;
+    uint32_t np = 0, nd = *ndel, nu = 0;
+    for (uint32_t p1 = 0; p1 < C; ++p1) {
+        if (!(ct.alive[p1] && ct.mask[p1])) continue;
+        for (uint32_t k = off[p1]; k < off[p1] + cnt[p1]; ++k) {
+            uint8_t cd = code[k];
+            if (cd == 3) continue;
+            if (cd == 4) { ++nu; continue; }
+            uint32_t p2 = p2_of[k];
+            if (!ct.mask[p2] || cd != 1) continue;
+            ct.mask[p2] = 0;
+            pairs[2 * np] = p1;
+            pairs[2 * np + 1] = p2;
+            ++np;
+            del_keys[nd++] = ct.key[p2];
+        }
+    }
+    *npairs = np;
+    *ndel = nd;
+    *nunknown += nu;
+}
+
+// Waves of predators: a predator that eats an earlier predator waits for it.
+__global__ void k_waves(uint32_t np, const uint32_t *pairs, uint32_t C, uint32_t *wave_of_slot, uint32_t *pred_list, uint32_t *pred_first,
+                        uint32_t *pred_count, uint32_t *pred_wave, uint32_t *npred, uint32_t *nwaves) {
+    if (threadIdx.x || blockIdx.x) return;
+    uint32_t n = 0, maxw = 0;
+    for (uint32_t k = 0; k < np;) {
+        uint32_t p = pairs[2 * k];
+        uint32_t first = k, w = 0;
+        while (k < np && pairs[2 * k] == p) {
+            uint32_t prey = pairs[2 * k + 1];
+            if (wave_of_slot[prey] != kNone) w = max(w, wave_of_slot[prey] + 1);
+            ++k;
+        }
+        wave_of_slot[p] = w;
+        pred_list[n] = p;
+        pred_first[n] = first;
+        pred_count[n] = k - first;
+        pred_wave[n] = w;
+        maxw = max(maxw, w);
+        ++n;
+    }
+    *npred = n;
+    *nwaves = np ? maxw + 1 : 0;
+}
+
+// MergeAnotherPlanetesimal for every predator of one wave (src/tree.hpp:4532-4611): the
+// scalar chain on thread 0, the members copied into a fresh segment (predator first, then
+// each prey in order); distances, sort and radii follow for the merged clumps.
+__global__ void k_merge(uint32_t npred, const uint32_t *pred_list, const uint32_t *pred_first, const uint32_t *pred_count,
+                        const uint32_t *pred_wave, uint32_t wave, const uint32_t *pairs, CT ct, Pool P, const double *dens, uint32_t *merged,
+                        uint32_t *nmerged, unsigned *err) {
+    __shared__ uint32_t s_off, s_tot, s_ok;
+    uint32_t t = blockIdx.x;
+    if (t >= npred || pred_wave[t] != wave) return;
+    uint32_t a = pred_list[t];
+    if (threadIdx.x == 0) {
+        double M = ct.M[a];
+        double4_32a c = ct.com[a], v = ct.vcom[a];
+        uint32_t peak = ct.peak[a], tot = ct.mn[a];
+        s_ok = 1;
+        for (uint32_t k = pred_first[t]; k < pred_first[t] + pred_count[t]; ++k) {
+            uint32_t b = pairs[2 * k + 1];
+            uint32_t sub;
+            if (dens[peak] < dens[ct.peak[b]]) {
+                sub = peak;
+                peak = ct.peak[b];
+            } else {
+                sub = ct.peak[b];
+            }
+            uint32_t e = atomicAdd(P.sub_top, 1u);
+            if (e < P.sub_cap) {
+                P.sub_peak[e] = sub;
+                P.sub_next[e] = kNone;
+                if (ct.sub_tail[a] == kNone) ct.sub_head[a] = e;
+                else P.sub_next[ct.sub_tail[a]] = e;
+                ct.sub_tail[a] = e;
+            } else {
+                atomicOr(err, (unsigned)kDevErrCapacity);
+            }
+            double Mb = ct.M[b];
+            double4_32a cb = ct.com[b], vb = ct.vcom[b];
+            double Mt = M + Mb;
+            c = make_double4_32a((c.x * M + cb.x * Mb) / Mt, (c.y * M + cb.y * Mb) / Mt, (c.z * M + cb.z * Mb) / Mt, 0);
+            v = make_double4_32a((v.x * M + vb.x * Mb) / Mt, (v.y * M + vb.y * Mb) / Mt, (v.z * M + vb.z * Mb) / Mt, 0);
+            M = Mt;
+            tot += ct.mn[b];
+        }
+        ct.M[a] = M;
+        ct.com[a] = c;
+        ct.vcom[a] = v;
+        ct.peak[a] = peak;
+        uint32_t o = pool_alloc(P, tot, err);
+        if (o == kNone) s_ok = 0;
+        s_off = o;
+        s_tot = tot;
+    }
+    __syncthreads();
+    if (!s_ok) return;
+    uint32_t at = s_off;
+    // predator first, then preys in order
+    {
+        const uint32_t o = ct.moff[a], m = ct.mn[a];
+        for (uint32_t k = threadIdx.x; k < m; k += blockDim.x) P.idx[at + k] = P.idx[o + k];
+        at += m;
+    }
+    for (uint32_t k = pred_first[t]; k < pred_first[t] + pred_count[t]; ++k) {
+        uint32_t b = pairs[2 * k + 1];
+        const uint32_t o = ct.moff[b], m = ct.mn[b];
+        for (uint32_t j = threadIdx.x; j < m; j += blockDim.x) P.idx[at + j] = P.idx[o + j];
+        at += m;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ct.moff[a] = s_off;
+        ct.mn[a] = s_tot;
+        merged[atomicAdd(nmerged, 1u)] = a;
+    }
+}
+
+// Re-key every clump to its densest sub-peak in key order (src/tree.hpp:4156-4182).
+__global__ void k_rekey(uint32_t C, CT ct, const uint32_t *order, uint32_t n, Pool P, const double *dens, uint32_t *slot_of_key,
+                        uint32_t *nfail) {
+    if (threadIdx.x || blockIdx.x) return;
+    // decisions first (all against the keys before re-keying), then the re-insertions
+    uint32_t fails = 0;
+    for (uint32_t r = 0; r < n; ++r) {
+        uint32_t s = order[r];
+        uint32_t best = ct.key[s];
+        for (uint32_t e = ct.sub_head[s]; e != kNone; e = P.sub_next[e])
+            if (dens[best] < dens[P.sub_peak[e]]) best = P.sub_peak[e];
+        ct.peak[s] = best;  // staged in peak; applied below
+    }
+    for (uint32_t r = 0; r < n; ++r) {
+        uint32_t s = order[r];
+        uint32_t nk = ct.peak[s], ok = ct.key[s];
+        if (nk == ok) continue;
+        if (slot_of_key[nk] != kNone) { ++fails; ct.peak[s] = ok; continue; }  // emplace fails: keep the old key
+        slot_of_key[ok] = kNone;
+        slot_of_key[nk] = s;
+        ct.key[s] = nk;
+    }
+    *nfail += fails;
+}
+
+// RemoveUnboundParticles (src/tree.hpp:4615-4674) for a list of clumps, one block each.
+__global__ void __launch_bounds__(256) k_unbind(const uint32_t *list, CT ct, Pool P, const double4_32a *pos, const double4_32a *vel, CP cp) {
+    __shared__ double sM, scx, scy, scz, svx, svy, svz;
+    __shared__ int s_best;
+    __shared__ uint32_t s_back;
+    uint32_t s = list[blockIdx.x];
+    const uint32_t o = ct.moff[s];
+    if (threadIdx.x == 0) {
+        sM = ct.M[s];
+        double4_32a c = ct.com[s], v = ct.vcom[s];
+        scx = c.x; scy = c.y; scz = c.z;
+        svx = v.x; svy = v.y; svz = v.z;
+        s_back = ct.mn[s] - 1;
+    }
+    __syncthreads();
+    int i = (int)ct.mn[s] - 1;
+    while (i >= 1) {
+        int lo = max(1, i - (int)blockDim.x + 1);
+        if (threadIdx.x == 0) s_best = -1;
+        __syncthreads();
+        int j = i - (int)threadIdx.x;
+        bool unbound = false;
+        double Mr = 0;
+        if (j >= lo) {
+            uint32_t pi = P.idx[o + j];
+            double4_32a p = pos[pi], v = vel[pi];
+            double M = sM;
+            Mr = M - p.w;
+            double cx = (scx * M - p.x * p.w) / Mr, cy = (scy * M - p.y * p.w) / Mr, cz = (scz * M - p.z * p.w) / Mr;
+            double vx = (svx * M - v.x * p.w) / Mr, vy = (svy * M - v.y * p.w) / Mr, vz = (svz * M - v.z * p.w) / Mr;
+            double dx = cx - p.x;
+            double ex = (vx - 0.0 * dx) - v.x, ey = (vy - cp.shear * dx) - v.y, ez = (vz - 0.0 * dx) - v.z;
+            double e = +0.5 / M * norm2_3(ex, ey, ez) - cp.G / norm3(cx - p.x, cy - p.y, cz - p.z);
+            unbound = e > 0;
+        }
+        if (unbound) atomicMax(&s_best, j);
+        __syncthreads();
+        int b = s_best;
+        if (b < 0) {
+            i = lo - 1;
+            __syncthreads();
+            continue;
+        }
+        if ((int)threadIdx.x == i - b) {  // the thread that evaluated b updates the state
+            uint32_t pi = P.idx[o + b];
+            double4_32a p = pos[pi], v = vel[pi];
+            double M = sM;
+            double Mr2 = M - p.w;
+            scx = (scx * M - p.x * p.w) / Mr2; scy = (scy * M - p.y * p.w) / Mr2; scz = (scz * M - p.z * p.w) / Mr2;
+            svx = (svx * M - v.x * p.w) / Mr2; svy = (svy * M - v.y * p.w) / Mr2; svz = (svz * M - v.z * p.w) / Mr2;
+            sM = Mr2;
+            // swap with the back and pop (src/tree.hpp:4660-4663)
+            uint32_t bk = s_back;
+            uint32_t tmp = P.idx[o + b];
+            P.idx[o + b] = P.idx[o + bk];
+            P.idx[o + bk] = tmp;
+            s_back = bk - 1;
+        }
+        __syncthreads();
+        i = b - 1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ct.mn[s] = s_back + 1;
+        ct.M[s] = sM;
+        ct.com[s] = make_double4_32a(scx, scy, scz, 0);
+        ct.vcom[s] = make_double4_32a(svx, svy, svz, 0);
+    }
+}
+
+// Hill-sphere rebinding of one clump (src/tree.hpp:4678-4711): the ball search's node
+// ranges are walked in order; candidates are evaluated a chunk at a time against the
+// current state and the first bound one is taken.
+__global__ void k_ball_ranges(KTree t, double cx, double cy, double cz, double r, uint32_t *rb, uint32_t *re, uint8_t *rpart, uint32_t cap,
+                              uint32_t *nr, uint32_t *ncand, unsigned *err) {
+    if (threadIdx.x || blockIdx.x) return;
+    uint32_t n = 0, tot = 0;
+    traverse(t, cx, cy, cz, r,
+             [&](uint32_t b, uint32_t e, bool partial) {
+                 if (n < cap) { rb[n] = b; re[n] = e; rpart[n] = partial ? 1 : 0; }
+                 ++n;
+                 tot += e - b;
+                 return true;
+             },
+             err);
+    if (n > cap) atomicOr(err, (unsigned)kDevErrCapacity);
+    *nr = min(n, cap);
+    *ncand = tot;
+}
+
+__global__ void __launch_bounds__(256) k_rebind(uint32_t s, CT ct, Pool P, const double4_32a *pos, const double4_32a *vel, const double *dens,
+                                                uint8_t *in_clump, const uint32_t *rb, const uint32_t *re, const uint8_t *rpart,
+                                                const uint32_t *nr_p, double cx0, double cy0, double cz0, double r, CP cp,
+                                                uint32_t *acc, uint32_t acc_cap, uint32_t *grew, unsigned *err) {
+    __shared__ double sM, scx, scy, scz, svx, svy, svz;
+    __shared__ uint32_t s_nacc, s_first, s_ri, s_rk, s_len, s_noff;
+    __shared__ uint32_t chunk[256];
+    __shared__ uint8_t cpart[256];
+    const uint32_t nr = *nr_p;
+    if (threadIdx.x == 0) {
+        sM = ct.M[s];
+        double4_32a c = ct.com[s], v = ct.vcom[s];
+        scx = c.x; scy = c.y; scz = c.z;
+        svx = v.x; svy = v.y; svz = v.z;
+        s_nacc = 0;
+        s_ri = 0;
+        s_rk = 0;
+    }
+    __syncthreads();
+    const double rr = r * r;
+    for (;;) {
+        // the next chunk of candidates in ball-search order (thread 0 walks the ranges)
+        if (threadIdx.x == 0) {
+            uint32_t len = 0, ri = s_ri, rk = s_rk;
+            while (len < blockDim.x && ri < nr) {
+                uint32_t b = rb[ri], e = re[ri];
+                if (b + rk >= e) { ++ri; rk = 0; continue; }
+                chunk[len] = b + rk;
+                cpart[len] = rpart[ri];
+                ++len;
+                ++rk;
+            }
+            s_len = len;
+            s_first = kNone;
+        }
+        __syncthreads();
+        const uint32_t len = s_len;
+        if (len == 0) break;
+        bool bound = false;
+        if (threadIdx.x < len) {
+            uint32_t q = chunk[threadIdx.x];
+            double4_32a p = pos[q], v = vel[q];
+            // RecursiveBallSearch keeps leaf points within r (contained nodes pass whole)
+            bool inside = !cpart[threadIdx.x] || point_dr2(cx0, cy0, cz0, p) <= rr;
+            if (inside && !in_clump[q] && !(dens[q] < cp.thr)) {
+                double M = sM + p.w;
+                double dx = scx - p.x;
+                double ex = (svx - 0.0 * dx) - v.x, ey = (svy - cp.shear * dx) - v.y, ez = (svz - 0.0 * dx) - v.z;
+                double e = +0.5 / M * norm2_3(ex, ey, ez) - cp.G / norm3(scx - p.x, scy - p.y, scz - p.z);
+                bound = e < 0;
+            }
+        }
+        if (bound) atomicMin(&s_first, threadIdx.x);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const uint32_t f = s_first;
+            const uint32_t adv = (f == kNone) ? len : f + 1;
+            if (f != kNone) {  // take it and update the state (src/tree.hpp:4696-4701)
+                uint32_t q = chunk[f];
+                double4_32a p = pos[q], v = vel[q];
+                double M = sM + p.w;
+                scx = (scx * M + p.w * p.x) / M; scy = (scy * M + p.w * p.y) / M; scz = (scz * M + p.w * p.z) / M;
+                svx = (M * svx + p.w * v.x) / M; svy = (M * svy + p.w * v.y) / M; svz = (M * svz + p.w * v.z) / M;
+                sM = M;
+                in_clump[q] = 1;
+                if (s_nacc < acc_cap) acc[s_nacc] = q;
+                else atomicOr(err, (unsigned)kDevErrCapacity);
+                s_nacc = s_nacc + 1;
+            }
+            uint32_t ri = s_ri, rk = s_rk, left = adv;
+            while (left > 0 && ri < nr) {
+                uint32_t b = rb[ri], e = re[ri];
+                uint32_t avail = (b + rk < e) ? e - (b + rk) : 0;
+                if (avail == 0) { ++ri; rk = 0; continue; }
+                uint32_t take = min(avail, left);
+                rk += take;
+                left -= take;
+            }
+            s_ri = ri;
+            s_rk = rk;
+        }
+        __syncthreads();
+    }
+    // new segment: previous members in order, then the accepted ones in acceptance order
+    const uint32_t nacc = min(s_nacc, acc_cap), m0 = ct.mn[s], o = ct.moff[s];
+    if (threadIdx.x == 0) s_noff = nacc ? pool_alloc(P, m0 + nacc, err) : o;
+    __syncthreads();
+    const uint32_t no = s_noff;
+    if (no == kNone) return;
+    if (nacc) {
+        for (uint32_t k = threadIdx.x; k < m0; k += blockDim.x) P.idx[no + k] = P.idx[o + k];
+        for (uint32_t k = threadIdx.x; k < nacc; k += blockDim.x) P.idx[no + m0 + k] = acc[k];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        *grew = nacc ? 1u : 0u;
+        ct.moff[s] = no;
+        ct.mn[s] = m0 + nacc;
+        ct.M[s] = sM;
+        ct.com[s] = make_double4_32a(scx, scy, scz, 0);
+        ct.vcom[s] = make_double4_32a(svx, svy, svz, 0);
+    }
+}
+
+__global__ void k_mark_members(uint32_t C, CT ct, Pool P, uint8_t *in_clump) {
+    uint32_t s = blockIdx.x;
+    if (s >= C || !ct.alive[s]) return;
+    for (uint32_t k = threadIdx.x; k < ct.mn[s]; k += blockDim.x) in_clump[P.idx[ct.moff[s] + k]] = 1;
+}
+
+// RemoveSmallMassAndLowPeak (src/tree.hpp:3524-3546)
+__global__ void k_prune(uint32_t C, CT ct, Pool P, const double4_32a *vel, const double *dens, CP cp, uint8_t *kill) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= C) return;
+    kill[s] = 0;
+    if (!ct.alive[s]) return;
+    if (ct.M[s] < cp.mass_thr || dens[ct.key[s]] < cp.peak_thr) { kill[s] = 1; return; }
+    uint32_t lim = min(ct.mn[s], cp.knn);
+    double m = 0;
+    for (uint32_t k = 0; k < lim; ++k) {
+        double a = vel[P.idx[ct.moff[s] + k]].w;
+        m = (m < a) ? a : m;
+    }
+    if (m < cp.peak_thr) kill[s] = 1;
+}
+
+// envelope rip step (src/tree.hpp:4231-4239)
+__global__ void k_rip(uint32_t C, CT ct, Pool P, uint8_t *pending, uint32_t *changed, uint32_t *nchanged) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= C || !ct.alive[s] || !pending[s]) return;
+    const uint32_t o = ct.moff[s], m = ct.mn[s];
+    if (m == 0) { pending[s] = 0; return; }
+    double h = ct.hill[s];
+    if (!(h < P.dist[o + m - 1])) { pending[s] = 0; return; }
+    uint32_t lo = 0, hi = m;  // first member with distance >= h
+    while (lo < hi) {
+        uint32_t mid = (lo + hi) / 2;
+        if (P.dist[o + mid] < h) lo = mid + 1;
+        else hi = mid;
+    }
+    if (lo == 0) { ct.alive[s] = 0; pending[s] = 0; return; }
+    ct.mn[s] = lo;
+    changed[atomicAdd(nchanged, 1u)] = s;
+}
+
+// CalculateAngularMomentum sums (src/tree.hpp:4721-4747), unnormalised
+__global__ void k_angmom(const uint32_t *list, uint32_t n, CT ct, Pool P, const double4_32a *pos, const double4_32a *vel, CP cp) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    uint32_t s = list[t];
+    const uint32_t o = ct.moff[s], m = ct.mn[s];
+    double4_32a c = ct.com[s], vc = ct.vcom[s];
+    double jx = 0, jy = 0, jz = 0;
+    for (uint32_t k = 0; k < m; ++k) {
+        uint32_t i = P.idx[o + k];
+        double4_32a p = pos[i], v = vel[i];
+        double drx = p.x - c.x, dry = p.y - c.y, drz = p.z - c.z;
+        double sx = 0. * p.x, sy = cp.shear * p.x, sz = 0. * p.x;
+        double cx0 = 0. * c.x, cy0 = cp.shear * c.x, cz0 = 0. * c.x;
+        double dvx = (v.x - sx) - (vc.x - cx0), dvy = (v.y - sy) - (vc.y - cy0), dvz = (v.z - sz) - (vc.z - cz0);
+        double tx = dry * dvz - drz * dvy, ty = drz * dvx - drx * dvz, tz = drx * dvy - dry * dvx;
+        double ax = -drx * drz, ay = -dry * drz, az = (drx * drx + dry * dry);
+        tx = tx + cp.Omega * ax; ty = ty + cp.Omega * ay; tz = tz + cp.Omega * az;
+        jx = jx + p.w * tx; jy = jy + p.w * ty; jz = jz + p.w * tz;
+    }
+    ct.J[s] = make_double4_32a(jx, jy, jz, 0);
+}
+
+// output gather: per final clump member (particles order): tree index -> pos/vel/orig,
+// and the number of offset sources (sink particles expand)
+__global__ void k_out_counts(const uint32_t *list, uint32_t nl, const uint32_t *base, CT ct, Pool P, const uint32_t *sink_n,
+                             uint32_t *ocnt) {
+    uint32_t t = blockIdx.x;
+    if (t >= nl) return;
+    uint32_t s = list[t];
+    for (uint32_t k = threadIdx.x; k < ct.mn[s]; k += blockDim.x) ocnt[base[t] + k] = sink_n[P.idx[ct.moff[s] + k]];
+}
+
+__global__ void k_out_fill(const uint32_t *list, uint32_t nl, const uint32_t *base, CT ct, Pool P, const double4_32a *pos, const double4_32a *vel,
+                           const uint32_t *orig, const uint32_t *sink_n, const uint32_t *sink_first, const uint32_t *sorted_src,
+                           const double4_32a *in_pos, const uint32_t *obase, double *mpos, double *mvel, double *mmass, uint32_t *morig,
+                           double *opos) {
+    uint32_t t = blockIdx.x;
+    if (t >= nl) return;
+    uint32_t s = list[t];
+    for (uint32_t k = threadIdx.x; k < ct.mn[s]; k += blockDim.x) {
+        uint32_t i = P.idx[ct.moff[s] + k];
+        size_t g = base[t] + k;
+        double4_32a p = pos[i], v = vel[i];
+        mpos[3 * g] = p.x; mpos[3 * g + 1] = p.y; mpos[3 * g + 2] = p.z;
+        mvel[3 * g] = v.x; mvel[3 * g + 1] = v.y; mvel[3 * g + 2] = v.z;
+        mmass[g] = p.w;
+        morig[g] = orig[i];
+        uint32_t ob = obase[g], n = sink_n[i];
+        if (n <= 1) {
+            opos[3 * (size_t)ob] = p.x; opos[3 * (size_t)ob + 1] = p.y; opos[3 * (size_t)ob + 2] = p.z;
+        } else {
+            for (uint32_t j = 0; j < n; ++j) {
+                double4_32a q = in_pos[sorted_src[sink_first[i] + j]];
+                opos[3 * (size_t)(ob + j)] = q.x; opos[3 * (size_t)(ob + j) + 1] = q.y; opos[3 * (size_t)(ob + j) + 2] = q.z;
+            }
+        }
+    }
+}
+
+}  // namespace
+
+// ====================================================================== host orchestration
+namespace {
+
+struct Stage {
+    Context &c;
+    cudaStream_t s;
+    CT ct;
+    Pool P;
+    CP cp;
+    uint32_t C = 0;
+    uint32_t *slot_of_key = nullptr;
+    uint32_t *d_list = nullptr;   // scratch slot list (capacity C)
+    uint32_t *d_list2 = nullptr;
+    uint8_t *d_flag8 = nullptr;
+    uint32_t *d_u = nullptr;      // small device counters
+    const DevTree &tr;
+
+    Stage(Context &cc, cudaStream_t ss) : c(cc), s(ss), tr(cc.tree) {}
+
+    int sync() {
+        PLAN_CUDA(cudaStreamSynchronize(s));
+        return kOk;
+    }
+    template <class T> int down(std::vector<T> &h, const T *d, size_t n) {
+        h.resize(n);
+        if (n) PLAN_CUDA(cudaMemcpyAsync(h.data(), d, n * sizeof(T), cudaMemcpyDeviceToHost, s));
+        return sync();
+    }
+    int up_list(const std::vector<uint32_t> &h, uint32_t *d) {
+        if (!h.empty()) PLAN_CUDA(cudaMemcpyAsync(d, h.data(), h.size() * 4, cudaMemcpyHostToDevice, s));
+        return kOk;
+    }
+    // alive slots in key order
+    int live_order(std::vector<uint32_t> &order, bool need_mask = false) {
+        std::vector<uint32_t> key;
+        std::vector<uint8_t> alive, mask;
+        int rc = down(key, ct.key, C);
+        if (!rc) rc = down(alive, ct.alive, C);
+        if (!rc && need_mask) rc = down(mask, ct.mask, C);
+        if (rc) return rc;
+        order.clear();
+        for (uint32_t i = 0; i < C; ++i)
+            if (alive[i] && (!need_mask || mask[i])) order.push_back(i);
+        std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return key[a] < key[b]; });
+        return kOk;
+    }
+
+    int kinematics(const std::vector<uint32_t> &list) {
+        if (list.empty()) return kOk;
+        int rc = up_list(list, d_list);
+        if (rc) return rc;
+        k_kinematics<<<grid_for(list.size(), 64), 64, 0, s>>>(d_list, (uint32_t)list.size(), ct, P, tr.pos, tr.vel);
+        c.launches++;
+        PLAN_CUDA(cudaGetLastError());
+        return kOk;
+    }
+
+    // distances, sort, radii for the listed clumps (the tail of SortParticles / Merge)
+    int resort(const std::vector<uint32_t> &list) {
+        if (list.empty()) return kOk;
+        int rc = up_list(list, d_list);
+        if (rc) return rc;
+        const uint32_t n = (uint32_t)list.size();
+        k_dist<<<n, 256, 0, s>>>(d_list, ct, P, tr.pos);
+        k_sort_small<<<n, 1024, 0, s>>>(d_list, ct, P);
+        c.launches += 2;
+        // segments longer than the in-block sort go through the radix sort
+        std::vector<uint32_t> mn;
+        rc = down(mn, ct.mn, C);
+        if (rc) return rc;
+        std::vector<uint32_t> large, base;
+        uint64_t tot = 0;
+        for (uint32_t sl : list)
+            if (mn[sl] > (uint32_t)kSmallSort) { large.push_back(sl); base.push_back((uint32_t)tot); tot += mn[sl]; }
+        if (!large.empty()) {
+            Arena &S = c.scratch;
+            size_t mark = S.used;
+            uint32_t *w0 = S.get<uint32_t>(tot), *w1 = S.get<uint32_t>(tot), *w2 = S.get<uint32_t>(tot), *pay = S.get<uint32_t>(tot);
+            uint32_t *dl = S.get<uint32_t>(large.size()), *db = S.get<uint32_t>(large.size());
+            size_t sb = radix_sort96_scratch_bytes(tot);
+            void *scr = S.take(sb);
+            if (S.failed || !scr) { S.used = mark; return kErrOutOfMemory; }
+            PLAN_CUDA(cudaMemcpyAsync(dl, large.data(), large.size() * 4, cudaMemcpyHostToDevice, s));
+            PLAN_CUDA(cudaMemcpyAsync(db, base.data(), base.size() * 4, cudaMemcpyHostToDevice, s));
+            k_large_gather<<<(unsigned)large.size(), 256, 0, s>>>(dl, (uint32_t)large.size(), db, ct, P, w0, w1, w2, pay);
+            rc = radix_sort96(w0, w1, w2, pay, tot, scr, sb, s);
+            if (rc) { S.used = mark; return rc; }
+            k_large_scatter<<<(unsigned)large.size(), 256, 0, s>>>(dl, (uint32_t)large.size(), db, ct, P, w0, w1, pay);
+            c.launches += 2 + 36;
+            PLAN_CUDA(cudaGetLastError());
+            rc = sync();
+            S.used = mark;
+            if (rc) return rc;
+            rc = up_list(list, d_list);
+            if (rc) return rc;
+        }
+        k_one10th<<<n, 256, 0, s>>>(d_list, ct, P, tr.pos, tr.dens);
+        c.launches++;
+        PLAN_CUDA(cudaGetLastError());
+        return kOk;
+    }
+
+    int sort_particles(const std::vector<uint32_t> &list) {
+        int rc = kinematics(list);
+        if (!rc) rc = resort(list);
+        return rc;
+    }
+
+    int dispersion(const std::vector<uint32_t> &list, double tol, std::vector<uint8_t> &res) {
+        res.clear();
+        if (list.empty()) return kOk;
+        int rc = up_list(list, d_list);
+        if (rc) return rc;
+        k_dispersion<<<grid_for(list.size(), 64), 64, 0, s>>>(d_list, (uint32_t)list.size(), ct, P, tol, d_flag8);
+        c.launches++;
+        return down(res, d_flag8, list.size());
+    }
+
+    int hill(const std::vector<uint32_t> &list) {
+        if (list.empty()) return kOk;
+        int rc = up_list(list, d_list);
+        if (rc) return rc;
+        k_hill<<<grid_for(list.size(), 128), 128, 0, s>>>(d_list, (uint32_t)list.size(), ct, cp.G, cp.Omega);
+        c.launches++;
+        PLAN_CUDA(cudaGetLastError());
+        return kOk;
+    }
+
+    int unbind(const std::vector<uint32_t> &list) {
+        if (list.empty()) return kOk;
+        int rc = up_list(list, d_list);
+        if (rc) return rc;
+        k_unbind<<<(unsigned)list.size(), 256, 0, s>>>(d_list, ct, P, tr.pos, tr.vel, cp);
+        c.launches++;
+        PLAN_CUDA(cudaGetLastError());
+        return sort_particles(list);  // RemoveUnboundParticles ends with SortParticles
+    }
+};
+
+}  // namespace
+
+int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogue **out) {
+    cudaEvent_t ev[6];
+    for (auto &e : ev) cudaEventCreate(&e);
+    cudaEventRecord(ev[0], s);
+    const DevTree &tr = c.tree;
+    const uint32_t Tu = tr.Tu, N = c.n_input;
+    // kernel choice and thresholds (src/tree.hpp:3576-3660), host scalars
+    uint32_t horiz = p.box_resolution[0] * p.box_resolution[1];
+    if (tr.box.half_width < p.max_half_width + p.max_ghost_zone_width - 1e-16)
+        horiz = (uint32_t)std::pow(tr.box.half_width / p.cell_length[0] * ((tr.box.half_width - p.max_ghost_zone_width) / tr.box.half_width), 2.0);
+    if (!(N >= 4 * horiz)) {
+        c.last_error = "fewer than 4 particles per horizontal cell: the spline density kernel of the reference is not built yet";
+        return kErrUnsupported;
+    }
+    if (!p.fixed_hop && N >= 1.67e7) p.hop = 64;
+    const double PI = 3.14159265358979323846;
+    double thr = std::pow(p.Omega, 2.) / PI / p.grav_constant * 2.;
+    if (p.mass_total_code_units / N / p.cell_volume > thr / 4) thr *= 9. / 8.;
+    double rmin = std::min(std::min((double)p.box_resolution[0] / p.box_length[0], (double)p.box_resolution[1] / p.box_length[1]),
+                           (double)p.box_resolution[2] / p.box_length[2]);
+    unsigned hydro = (unsigned)rmin;
+    double diffuse = 0.55, hillf = 0.25;
+    if (hydro <= 1024) { diffuse = 0.35; hillf = 0.75; }
+    else if (hydro <= 1536) { diffuse = 0.4; hillf = 0.5; }
+    else if (hydro <= 2048) { diffuse = 0.5; hillf = 0.35; }
+    if (p.clump_diffuse_threshold > 0) diffuse = p.clump_diffuse_threshold;
+    if (p.Hill_fraction_for_merge > 0) hillf = p.Hill_fraction_for_merge;
+    if (p.knn < 1 || p.knn > 128 || p.hop < 1 || p.hop > 128 || p.knn > Tu || p.hop > Tu) {
+        c.last_error = "knn and hop must lie in [1, 128] and not exceed the number of tree points";
+        return kErrUnsupported;
+    }
+    c.fs = FindScalars{thr, 3 * thr, p.min_trusted_mass, diffuse, hillf, p.knn, p.hop, 1};
+
+    // 1-2. densities and densest neighbours
+    int rc = launch_density(c, p, p.knn, s);
+    if (rc) return rc;
+    cudaEventRecord(ev[1], s);
+    uint32_t *densest = c.arena.get<uint32_t>(Tu);
+    if (!densest) return kErrOutOfMemory;
+    c.densest = densest;
+    rc = launch_densest(c, p, p.hop, thr, densest, s);
+    if (rc) return rc;
+    cudaEventRecord(ev[2], s);
+    // 3. HOP groups
+    HopGroups hg;
+    rc = hop_groups(c, densest, thr, hg, s);
+    if (rc) return rc;
+    c.peak = hg.peak;
+    cudaEventRecord(ev[3], s);
+
+    // ------------------------------------------------------------------ clump stage
+    Stage st(c, s);
+    const uint32_t C = hg.n_groups;
+    st.C = C;
+    Arena &A = c.arena;
+    CT &ct = st.ct;
+    ct.C = C;
+    ct.key = A.get<uint32_t>(C + 1); ct.peak = A.get<uint32_t>(C + 1);
+    ct.mask = A.get<uint8_t>(C + 1); ct.alive = A.get<uint8_t>(C + 1);
+    ct.M = A.get<double>(C + 1);
+    ct.com = A.get<double4_32a>(C + 1); ct.vcom = A.get<double4_32a>(C + 1); ct.J = A.get<double4_32a>(C + 1);
+    ct.r_in = A.get<double>(C + 1); ct.r_out = A.get<double>(C + 1); ct.r10 = A.get<double>(C + 1);
+    ct.r2s = A.get<double>(C + 1); ct.hill = A.get<double>(C + 1);
+    ct.moff = A.get<uint32_t>(C + 1); ct.mn = A.get<uint32_t>(C + 1);
+    ct.sub_head = A.get<uint32_t>(C + 1); ct.sub_tail = A.get<uint32_t>(C + 1);
+    Pool &P = st.P;
+    const uint32_t m0 = hg.n_members;
+    P.cap = (uint32_t)std::min<uint64_t>(0xfffffff0ull, 4ull * m0 + Tu / 2 + 4096);
+    P.idx = A.get<uint32_t>(P.cap);
+    P.dist = A.get<double>(P.cap);
+    P.top = A.get<uint32_t>(4);
+    P.sub_cap = C + 16;
+    P.sub_peak = A.get<uint32_t>(P.sub_cap);
+    P.sub_next = A.get<uint32_t>(P.sub_cap);
+    P.sub_top = A.get<uint32_t>(4);
+    st.slot_of_key = A.get<uint32_t>(Tu);
+    st.d_list = A.get<uint32_t>(C + 1);
+    st.d_list2 = A.get<uint32_t>(C + 1);
+    st.d_flag8 = A.get<uint8_t>(C + 1);
+    st.d_u = A.get<uint32_t>(64);
+    uint8_t *in_clump = A.get<uint8_t>(Tu);
+    if (A.failed) return kErrOutOfMemory;
+    st.cp = CP{p.grav_constant, p.q * p.Omega, p.Omega, thr, 3 * thr, p.min_trusted_mass, diffuse, hillf, p.knn, Tu};
+    PLAN_CUDA(cudaMemsetAsync(st.slot_of_key, 0xff, (size_t)Tu * 4, s));
+    PLAN_CUDA(cudaMemsetAsync(st.d_u, 0, 64 * 4, s));
+    PLAN_CUDA(cudaMemsetAsync(P.sub_top, 0, 4, s));
+    PLAN_CUDA(cudaMemcpyAsync(P.idx, hg.members, (size_t)m0 * 4, cudaMemcpyDeviceToDevice, s));
+    PLAN_CUDA(cudaMemcpyAsync(P.top, &m0, 4, cudaMemcpyHostToDevice, s));
+    if (C) {
+        k_init<<<grid_for(C, 256), 256, 0, s>>>(C, hg.key, hg.off, ct, st.slot_of_key);
+        c.launches++;
+    }
+    c.counters[5] = m0;
+    c.counters[6] = C;
+    std::vector<uint32_t> all(C);
+    std::iota(all.begin(), all.end(), 0u);
+    // SortParticles + the diffuse cut after HOP (src/tree.hpp:3816-3829)
+    rc = st.sort_particles(all);
+    if (rc) return rc;
+    std::vector<uint8_t> too;
+    std::vector<uint32_t> del_keys_host;
+    if (diffuse < 0.525) {
+        rc = st.dispersion(all, diffuse, too);
+        if (rc) return rc;
+        std::vector<uint8_t> alive(C, 1);
+        for (uint32_t i = 0; i < C; ++i) if (too[i]) alive[i] = 0;
+        PLAN_CUDA(cudaMemcpyAsync(ct.alive, alive.data(), C, cudaMemcpyHostToDevice, s));
+    }
+    std::vector<uint32_t> live;
+    rc = st.live_order(live);
+    if (rc) return rc;
+    uint32_t num_planetesimals = (uint32_t)live.size();
+
+    // 4. merge sweeps (src/tree.hpp:3863-4152)
+    uint32_t *d_cnt = A.get<uint32_t>(C + 1), *d_off = A.get<uint32_t>(C + 1);
+    uint32_t *d_rank = A.get<uint32_t>(C + 1), *d_ctslot = A.get<uint32_t>(C + 1);
+    uint32_t *d_pairs = A.get<uint32_t>(2 * (size_t)C + 2), *d_del = A.get<uint32_t>(2 * (size_t)C + 2);
+    uint32_t *d_wave = A.get<uint32_t>(C + 1), *d_pl = A.get<uint32_t>(C + 1), *d_pf = A.get<uint32_t>(C + 1);
+    uint32_t *d_pc = A.get<uint32_t>(C + 1), *d_pw = A.get<uint32_t>(C + 1), *d_merged = A.get<uint32_t>(C + 1);
+    double4_32a *ct_pos = A.get<double4_32a>(C + 1), *ct_vel = A.get<double4_32a>(C + 1);
+    double *d_maxr = A.get<double>(2);
+    if (A.failed) return kErrOutOfMemory;
+    const size_t arena_mark = A.used;
+    uint32_t nunknown_total = 0, quirk = 0;
+    for (int kind = 0; kind < 2 && C; ++kind) {
+        const bool hill_mode = kind == 1;
+        if (hill_mode) {
+            rc = st.hill(live);
+            if (rc) return rc;
+        }
+        double max_radius = 0.;
+        const uint32_t start_num = num_planetesimals;
+        uint32_t delete_count = 0;
+        PLAN_CUDA(cudaMemsetAsync(st.d_u, 0, 64 * 4, s));  // [0] ndel, [1] npairs, [2] nunknown, ...
+        bool merged_any = true;
+        for (int sweep = 0; merged_any && sweep < 100000; ++sweep) {
+            A.used = arena_mark;  // per-sweep buffers (clump tree, candidates) are rebuilt
+            // BuildClumpTree over live clumps in key order (src/tree.hpp:5251-5284)
+            k_mark_live<<<grid_for(C, 256), 256, 0, s>>>(C, ct, d_cnt);
+            uint32_t *d_tot = st.d_u + 8;
+            size_t sb = scan_u32_scratch_bytes(C + 1);
+            const size_t smark = c.scratch.used;
+            void *scr = c.scratch.take(sb);
+            if (!scr) return kErrOutOfMemory;
+            rc = scan_u32(d_cnt, d_rank, C, d_tot, scr, sb, s);
+            c.scratch.used = smark;
+            if (rc) return rc;
+            k_ct_points<<<grid_for(C, 256), 256, 0, s>>>(C, ct, d_cnt, d_rank, p.mass_per_particle[0], ct_pos, ct_vel, d_ctslot);
+            k_max_radius<<<1, 1024, 0, s>>>(C, ct, hill_mode, hillf, d_maxr);
+            c.launches += 3;
+            uint32_t nct = 0;
+            double mr = 0;
+            PLAN_CUDA(cudaMemcpyAsync(&nct, d_tot, 4, cudaMemcpyDeviceToHost, s));
+            PLAN_CUDA(cudaMemcpyAsync(&mr, d_maxr, 8, cudaMemcpyDeviceToHost, s));
+            rc = st.sync();
+            if (rc) return rc;
+            if (nct != num_planetesimals) ++quirk;  // the reference sizes the clump set by this count
+            max_radius = std::max(mr, max_radius);
+            DevTree ctree;
+            if (nct) {
+                TreeBox box = make_box(tr.box.root_center, tr.box.half_width);
+                rc = build_octree(c, ct_pos, ct_vel, nullptr, nct, box, p.mass_per_particle, 1, ctree, s, nullptr);
+                if (rc) return rc;
+            }
+            KTree kct = ktree_of(ctree);
+            // candidates
+            uint32_t ncand = 0;
+            if (nct) {
+                k_ball_clumps<<<grid_for(C, 128), 128, 0, s>>>(0, C, ct, kct, hill_mode, hillf, max_radius, d_cnt, nullptr, nullptr, c.d_err);
+                const size_t sm2 = c.scratch.used;
+                void *scr2 = c.scratch.take(sb);
+                rc = scan_u32(d_cnt, d_off, C, d_tot, scr2, sb, s);
+                c.scratch.used = sm2;
+                if (rc) return rc;
+                PLAN_CUDA(cudaMemcpyAsync(&ncand, d_tot, 4, cudaMemcpyDeviceToHost, s));
+                rc = st.sync();
+                if (rc) return rc;
+                c.launches++;
+            }
+            uint32_t *d_cand = A.get<uint32_t>(ncand + 1), *d_cp1 = A.get<uint32_t>(ncand + 1), *d_p2 = A.get<uint32_t>(ncand + 1);
+            uint8_t *d_code = A.get<uint8_t>(ncand + 1);
+            double *d_sq = A.get<double>(3 * (size_t)ncand + 3), *d_sest = A.get<double>(ncand + 1), *d_sden = A.get<double>(ncand + 1);
+            uint32_t *d_sof = A.get<uint32_t>(ncand + 1);
+            if (A.failed) return kErrOutOfMemory;
+            uint32_t nsaddle = 0;
+            if (ncand) {
+                k_ball_clumps<<<grid_for(C, 128), 128, 0, s>>>(1, C, ct, kct, hill_mode, hillf, max_radius, d_cnt, d_off, d_cand, c.d_err);
+                // candidate -> predator slot
+                std::vector<uint32_t> hcnt, hoff;
+                rc = st.down(hcnt, d_cnt, C);
+                if (!rc) rc = st.down(hoff, d_off, C);
+                if (rc) return rc;
+                std::vector<uint32_t> cp1(ncand);
+                for (uint32_t sl = 0; sl < C; ++sl)
+                    for (uint32_t k = 0; k < hcnt[sl]; ++k) cp1[hoff[sl] + k] = sl;
+                PLAN_CUDA(cudaMemcpyAsync(d_cp1, cp1.data(), (size_t)ncand * 4, cudaMemcpyHostToDevice, s));
+                PLAN_CUDA(cudaMemsetAsync(st.d_u + 16, 0, 4, s));
+                k_pair_eval<<<grid_for(ncand, 128), 128, 0, s>>>(ncand, d_cp1, d_cand, ctree.in_vel, ct, st.slot_of_key, st.cp, hill_mode,
+                                                                 d_code, d_p2, d_sq, d_sest, d_sof, st.d_u + 16);
+                PLAN_CUDA(cudaMemcpyAsync(&nsaddle, st.d_u + 16, 4, cudaMemcpyDeviceToHost, s));
+                rc = st.sync();
+                if (rc) return rc;
+                c.launches += 2;
+                if (nsaddle) {
+                    rc = launch_density_at(c, d_sq, d_sest, nsaddle, p.knn, d_sden, s);
+                    if (rc) return rc;
+                    k_saddle_apply<<<grid_for(nsaddle, 128), 128, 0, s>>>(nsaddle, d_sof, d_sden, 2.5 * thr, d_code);
+                    c.launches++;
+                }
+            }
+            // serial resolution
+            PLAN_CUDA(cudaMemsetAsync(st.d_u + 1, 0, 4, s));
+            k_resolve<<<1, 1, 0, s>>>(C, ct, d_cnt, d_off, d_code, d_p2, d_pairs, st.d_u + 1, d_del, st.d_u + 0, st.d_u + 2);
+            c.launches++;
+            uint32_t h_u[3];
+            PLAN_CUDA(cudaMemcpyAsync(h_u, st.d_u, 12, cudaMemcpyDeviceToHost, s));
+            rc = st.sync();
+            if (rc) return rc;
+            const uint32_t npairs = h_u[1];
+            delete_count = h_u[0];
+            merged_any = npairs > 0;
+            if (npairs) {
+                PLAN_CUDA(cudaMemsetAsync(d_wave, 0xff, (size_t)(C + 1) * 4, s));
+                k_waves<<<1, 1, 0, s>>>(npairs, d_pairs, C, d_wave, d_pl, d_pf, d_pc, d_pw, st.d_u + 20, st.d_u + 21);
+                uint32_t hw[2];
+                PLAN_CUDA(cudaMemcpyAsync(hw, st.d_u + 20, 8, cudaMemcpyDeviceToHost, s));
+                rc = st.sync();
+                if (rc) return rc;
+                c.launches++;
+                const uint32_t npred = hw[0], nwaves = hw[1];
+                for (uint32_t w = 0; w < nwaves; ++w) {
+                    PLAN_CUDA(cudaMemsetAsync(st.d_u + 24, 0, 4, s));
+                    k_merge<<<npred, 256, 0, s>>>(npred, d_pl, d_pf, d_pc, d_pw, w, d_pairs, ct, P, tr.dens, d_merged, st.d_u + 24, c.d_err);
+                    c.launches++;
+                    std::vector<uint32_t> nm;
+                    rc = st.down(nm, st.d_u + 24, 1);
+                    if (rc) return rc;
+                    std::vector<uint32_t> merged;
+                    rc = st.down(merged, d_merged, nm[0]);
+                    if (rc) return rc;
+                    rc = st.resort(merged);
+                    if (rc) return rc;
+                    if (hill_mode) {
+                        rc = st.hill(merged);
+                        if (rc) return rc;
+                    }
+                }
+            }
+            // post-sweep diffuse test with the default tolerance (src/tree.hpp:3984-3992)
+            std::vector<uint32_t> masked;
+            rc = st.live_order(masked, true);
+            if (rc) return rc;
+            rc = st.dispersion(masked, 0.55, too);
+            if (rc) return rc;
+            std::vector<uint8_t> mask_now;
+            rc = st.down(mask_now, ct.mask, C);
+            if (rc) return rc;
+            std::vector<uint32_t> keys_now;
+            rc = st.down(keys_now, ct.key, C);
+            if (rc) return rc;
+            std::vector<uint32_t> extra_del;
+            for (size_t k = 0; k < masked.size(); ++k)
+                if (too[k]) { mask_now[masked[k]] = 0; extra_del.push_back(keys_now[masked[k]]); }
+            if (!extra_del.empty()) {
+                PLAN_CUDA(cudaMemcpyAsync(ct.mask, mask_now.data(), C, cudaMemcpyHostToDevice, s));
+                PLAN_CUDA(cudaMemcpyAsync(d_del + delete_count, extra_del.data(), extra_del.size() * 4, cudaMemcpyHostToDevice, s));
+                delete_count += (uint32_t)extra_del.size();
+                PLAN_CUDA(cudaMemcpyAsync(st.d_u + 0, &delete_count, 4, cudaMemcpyHostToDevice, s));
+            }
+            num_planetesimals = (uint32_t)live.size() - delete_count;
+            (hill_mode ? c.counters[12] : c.counters[11])++;
+        }
+        // erase the deleted clumps (and a clump keyed 0 when the zero-filled list has room,
+        // src/tree.hpp:3874, 4000-4002)
+        std::vector<uint32_t> dk;
+        rc = st.down(dk, d_del, delete_count);
+        if (rc) return rc;
+        std::vector<uint8_t> alive;
+        rc = st.down(alive, ct.alive, C);
+        if (rc) return rc;
+        std::vector<uint32_t> keys_now;
+        rc = st.down(keys_now, ct.key, C);
+        if (rc) return rc;
+        std::vector<uint32_t> sok(Tu, kNone);
+        for (uint32_t i = 0; i < C; ++i) if (alive[i]) sok[keys_now[i]] = i;
+        for (uint32_t k : dk) if (sok[k] != kNone) { alive[sok[k]] = 0; }
+        if (delete_count < start_num && sok[0] != kNone && alive[sok[0]]) { alive[sok[0]] = 0; ++quirk; }
+        std::vector<uint32_t> sok_dev(Tu, kNone);
+        for (uint32_t i = 0; i < C; ++i) if (alive[i]) sok_dev[keys_now[i]] = i;
+        PLAN_CUDA(cudaMemcpyAsync(ct.alive, alive.data(), C, cudaMemcpyHostToDevice, s));
+        PLAN_CUDA(cudaMemcpyAsync(st.slot_of_key, sok_dev.data(), (size_t)Tu * 4, cudaMemcpyHostToDevice, s));
+        rc = st.live_order(live);
+        if (rc) return rc;
+        num_planetesimals = (uint32_t)live.size() + ((delete_count < start_num && quirk) ? 0 : 0);
+        // all survivors are masked again by construction (every unmasked clump was deleted)
+    }
+    A.used = arena_mark;
+    c.counters[13] = quirk;
+    c.counters[14] = nunknown_total;
+    cudaEventRecord(ev[4], s);
+
+    // re-key (src/tree.hpp:4156-4182)
+    if (!live.empty()) {
+        int rc2 = st.up_list(live, st.d_list2);
+        if (rc2) return rc2;
+        k_rekey<<<1, 1, 0, s>>>(C, ct, st.d_list2, (uint32_t)live.size(), P, tr.dens, st.slot_of_key, st.d_u + 30);
+        c.launches++;
+        rc = st.live_order(live);
+        if (rc) return rc;
+    }
+    // 5. unbind, mark, rebind (src/tree.hpp:4189-4208)
+    rc = st.unbind(live);
+    if (!rc) rc = st.hill(live);
+    if (rc) return rc;
+    PLAN_CUDA(cudaMemsetAsync(in_clump, 0, Tu, s));
+    if (C) {
+        k_mark_members<<<C, 256, 0, s>>>(C, ct, P, in_clump);
+        c.launches++;
+    }
+    {
+        const uint32_t rcap = 1u << 20;
+        const uint32_t acc_cap = Tu;
+        uint32_t *rb = A.get<uint32_t>(rcap), *re = A.get<uint32_t>(rcap), *acc = A.get<uint32_t>(acc_cap);
+        uint8_t *rpart = A.get<uint8_t>(rcap);
+        if (A.failed) return kErrOutOfMemory;
+        KTree kt = ktree_of(tr);
+        std::vector<double4_32a> com1(1);
+        std::vector<double> h1(1);
+        for (uint32_t sl : live) {
+            for (int iter = 0; iter < 100000; ++iter) {
+                rc = st.down(com1, ct.com + sl, 1);
+                if (!rc) rc = st.down(h1, ct.hill + sl, 1);
+                if (rc) return rc;
+                k_ball_ranges<<<1, 1, 0, s>>>(kt, com1[0].x, com1[0].y, com1[0].z, h1[0], rb, re, rpart, rcap, st.d_u + 40, st.d_u + 41, c.d_err);
+                k_rebind<<<1, 256, 0, s>>>(sl, ct, P, tr.pos, tr.vel, tr.dens, in_clump, rb, re, rpart, st.d_u + 40, com1[0].x, com1[0].y,
+                                           com1[0].z, h1[0], st.cp, acc, acc_cap, st.d_u + 42, c.d_err);
+                c.launches += 2;
+                std::vector<uint32_t> g;
+                rc = st.down(g, st.d_u + 42, 1);
+                if (rc) return rc;
+                std::vector<uint32_t> one{sl};
+                if (g[0]) {
+                    rc = st.sort_particles(one);
+                    if (rc) return rc;
+                }
+                rc = st.hill(one);
+                if (rc) return rc;
+                if (!g[0]) break;
+            }
+        }
+    }
+    // 6. prune and loose streams (src/tree.hpp:4213-4224)
+    auto prune = [&]() -> int {
+        if (!C) return kOk;
+        k_prune<<<grid_for(C, 128), 128, 0, s>>>(C, ct, P, tr.vel, tr.dens, st.cp, st.d_flag8);
+        c.launches++;
+        std::vector<uint8_t> kill, alive;
+        int r = st.down(kill, st.d_flag8, C);
+        if (!r) r = st.down(alive, ct.alive, C);
+        if (r) return r;
+        for (uint32_t i = 0; i < C; ++i) if (kill[i]) alive[i] = 0;
+        PLAN_CUDA(cudaMemcpyAsync(ct.alive, alive.data(), C, cudaMemcpyHostToDevice, s));
+        return st.live_order(live);
+    };
+    rc = prune();
+    if (rc) return rc;
+    {
+        rc = st.dispersion(live, std::min(diffuse + 0.1, 0.475), too);
+        if (rc) return rc;
+        std::vector<uint8_t> alive;
+        rc = st.down(alive, ct.alive, C);
+        if (rc) return rc;
+        for (size_t k = 0; k < live.size(); ++k) if (too[k]) alive[live[k]] = 0;
+        PLAN_CUDA(cudaMemcpyAsync(ct.alive, alive.data(), C, cudaMemcpyHostToDevice, s));
+        rc = st.live_order(live);
+        if (rc) return rc;
+    }
+    // 7. rip the envelope (src/tree.hpp:4229-4248)
+    {
+        uint8_t *pending = A.get<uint8_t>(C + 1);
+        if (!pending) return kErrOutOfMemory;
+        PLAN_CUDA(cudaMemsetAsync(pending, 1, C + 1, s));
+        for (int round = 0; round < 100000 && C; ++round) {
+            PLAN_CUDA(cudaMemsetAsync(st.d_u + 50, 0, 4, s));
+            k_rip<<<grid_for(C, 128), 128, 0, s>>>(C, ct, P, pending, st.d_list2, st.d_u + 50);
+            c.launches++;
+            std::vector<uint32_t> nch;
+            rc = st.down(nch, st.d_u + 50, 1);
+            if (rc) return rc;
+            if (!nch[0]) break;
+            std::vector<uint32_t> changed;
+            rc = st.down(changed, st.d_list2, nch[0]);
+            if (rc) return rc;
+            rc = st.kinematics(changed);
+            if (!rc) rc = st.unbind(changed);
+            if (!rc) rc = st.hill(changed);
+            if (rc) return rc;
+        }
+        rc = st.live_order(live);
+        if (rc) return rc;
+    }
+    // 8-9. prune again; ghost clumps (src/tree.hpp:4253-4266)
+    rc = prune();
+    if (rc) return rc;
+    {
+        std::vector<double4_32a> com;
+        std::vector<uint8_t> alive;
+        rc = st.down(com, ct.com, C);
+        if (!rc) rc = st.down(alive, ct.alive, C);
+        if (rc) return rc;
+        for (uint32_t sl : live) {
+            double x[3] = {com[sl].x, com[sl].y, com[sl].z};
+            bool in = true;
+            for (int d = 0; d < 3; ++d) in = in && (x[d] >= p.box_min[d] && x[d] <= p.box_max[d]);
+            if (!in) alive[sl] = 0;
+        }
+        PLAN_CUDA(cudaMemcpyAsync(ct.alive, alive.data(), C, cudaMemcpyHostToDevice, s));
+        rc = st.live_order(live);
+        if (rc) return rc;
+    }
+    // 10. angular momentum (src/tree.hpp:4273-4275)
+    if (!live.empty()) {
+        rc = st.up_list(live, st.d_list);
+        if (rc) return rc;
+        k_angmom<<<grid_for(live.size(), 64), 64, 0, s>>>(st.d_list, (uint32_t)live.size(), ct, P, tr.pos, tr.vel, st.cp);
+        c.launches++;
+    }
+    cudaEventRecord(ev[5], s);
+
+    // ------------------------------------------------------------------ catalogue
+    plan_catalogue *cat = new plan_catalogue();
+    cat->time = c.time;
+    cat->mass_total_code_units = p.mass_total_code_units;
+    cat->mass_physical = p.mass_physical;
+    cat->grav_constant = p.grav_constant;
+    cat->Omega = p.Omega;
+    const uint32_t nl = (uint32_t)live.size();
+    std::vector<uint32_t> keys, mn;
+    std::vector<double> M;
+    std::vector<double4_32a> com, vcom, J;
+    rc = st.down(keys, ct.key, C);
+    if (!rc) rc = st.down(mn, ct.mn, C);
+    if (!rc) rc = st.down(M, ct.M, C);
+    if (!rc) rc = st.down(com, ct.com, C);
+    if (!rc) rc = st.down(vcom, ct.vcom, C);
+    if (!rc) rc = st.down(J, ct.J, C);
+    if (rc) { delete cat; return rc; }
+    std::vector<uint32_t> base(nl + 1, 0);
+    for (uint32_t t = 0; t < nl; ++t) base[t + 1] = base[t] + mn[live[t]];
+    const uint32_t tot = base[nl];
+    if (nl) {
+        uint32_t *dl = A.get<uint32_t>(nl), *db = A.get<uint32_t>(nl + 1), *ocnt = A.get<uint32_t>(tot + 1), *obase = A.get<uint32_t>(tot + 1);
+        uint32_t *d_otot = A.get<uint32_t>(2);
+        if (A.failed) { delete cat; return kErrOutOfMemory; }
+        PLAN_CUDA(cudaMemcpyAsync(dl, live.data(), nl * 4, cudaMemcpyHostToDevice, s));
+        PLAN_CUDA(cudaMemcpyAsync(db, base.data(), (nl + 1) * 4, cudaMemcpyHostToDevice, s));
+        k_out_counts<<<nl, 256, 0, s>>>(dl, nl, db, ct, P, tr.sink_n, ocnt);
+        const size_t sm3 = c.scratch.used;
+        size_t sb = scan_u32_scratch_bytes(tot + 1);
+        void *scr = c.scratch.take(sb);
+        if (!scr) { delete cat; return kErrOutOfMemory; }
+        rc = scan_u32(ocnt, obase, tot, d_otot, scr, sb, s);
+        c.scratch.used = sm3;
+        if (rc) { delete cat; return rc; }
+        uint32_t otot = 0;
+        PLAN_CUDA(cudaMemcpyAsync(&otot, d_otot, 4, cudaMemcpyDeviceToHost, s));
+        rc = st.sync();
+        if (rc) { delete cat; return rc; }
+        double *mpos = A.get<double>(3 * (size_t)tot + 3), *mvel = A.get<double>(3 * (size_t)tot + 3), *mmass = A.get<double>(tot + 1);
+        uint32_t *morig = A.get<uint32_t>(tot + 1);
+        double *opos = A.get<double>(3 * (size_t)otot + 3);
+        if (A.failed) { delete cat; return kErrOutOfMemory; }
+        k_out_fill<<<nl, 256, 0, s>>>(dl, nl, db, ct, P, tr.pos, tr.vel, tr.orig, tr.sink_n, tr.sink_first, tr.sorted_src, tr.in_pos, obase,
+                                      mpos, mvel, mmass, morig, opos);
+        c.launches += 3;
+        std::vector<double> hpos, hvel, hmass, hopos;
+        std::vector<uint32_t> horig, hob;
+        rc = st.down(hpos, mpos, 3 * (size_t)tot);
+        if (!rc) rc = st.down(hvel, mvel, 3 * (size_t)tot);
+        if (!rc) rc = st.down(hmass, mmass, tot);
+        if (!rc) rc = st.down(horig, morig, tot);
+        if (!rc) rc = st.down(hopos, opos, 3 * (size_t)otot);
+        if (!rc) rc = st.down(hob, obase, tot);
+        if (rc) { delete cat; return rc; }
+        cat->clumps.resize(nl);
+        for (uint32_t t = 0; t < nl; ++t) {
+            uint32_t sl = live[t];
+            auto &k = cat->clumps[t];
+            k.key = keys[sl];
+            k.M = M[sl];
+            k.com[0] = com[sl].x; k.com[1] = com[sl].y; k.com[2] = com[sl].z;
+            k.vcom[0] = vcom[sl].x; k.vcom[1] = vcom[sl].y; k.vcom[2] = vcom[sl].z;
+            k.Jsum[0] = J[sl].x; k.Jsum[1] = J[sl].y; k.Jsum[2] = J[sl].z;
+            uint32_t b = base[t], n = mn[sl];
+            k.orig.assign(horig.begin() + b, horig.begin() + b + n);
+            k.pos.assign(hpos.begin() + 3 * (size_t)b, hpos.begin() + 3 * (size_t)(b + n));
+            k.vel.assign(hvel.begin() + 3 * (size_t)b, hvel.begin() + 3 * (size_t)(b + n));
+            k.mass.assign(hmass.begin() + b, hmass.begin() + b + n);
+            uint32_t ob = hob[b], oe = (t + 1 < nl) ? hob[base[t + 1]] : otot;
+            k.opos.assign(hopos.begin() + 3 * (size_t)ob, hopos.begin() + 3 * (size_t)oe);
+            k.npar = oe - ob;
+        }
+        cat->have_members = true;
+    }
+    finish_catalogue(*cat, p.num_peaks);  // ranking, cap, host-libm values, summary
+    rc = st.sync();
+    if (rc) { delete cat; return rc; }
+    float ms;
+    cudaEventElapsedTime(&ms, ev[0], ev[1]); c.stage_ms[4] = ms;
+    cudaEventElapsedTime(&ms, ev[1], ev[2]); c.stage_ms[5] = ms;
+    cudaEventElapsedTime(&ms, ev[2], ev[3]); c.stage_ms[6] = ms;
+    cudaEventElapsedTime(&ms, ev[3], ev[5]); c.stage_ms[7] = ms;
+    for (auto &e : ev) cudaEventDestroy(e);
+    c.counters[7] = cat->clumps.size();
+    if (out) *out = cat;
+    else delete cat;
+    return kOk;
+}
+
+}  // namespace plan
