@@ -5,6 +5,7 @@
 #include <cerrno>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <iomanip>
@@ -989,6 +990,8 @@ std::string Finder::find(uint32_t num_in) {
                 }
             }
             if (!pairs.empty()) merged = true;
+            if (std::getenv("PLAN_DEBUG_MERGES"))
+                for (auto &pr : pairs) std::fprintf(stderr, "merge kind %d pred %u prey %u\n", sweep_kind, pr.first, pr.second);
             // predators in key order, each eating its preys in ball-search order
             for (size_t k = 0; k < pairs.size(); ++k) {
                 Clump &pred = clumps[pairs[k].first];
@@ -1011,6 +1014,12 @@ std::string Finder::find(uint32_t num_in) {
     }
     // re-key to the densest sub-peak, src/tree.hpp:4156-4182
     std::vector<uint32_t> old_keys, new_keys;
+    if (std::getenv("PLAN_DEBUG_MERGES"))
+        for (auto &it : clumps) {
+            std::fprintf(stderr, "clump %u peak %u subs", it.first, it.second.peak_index);
+            for (uint32_t o : it.second.potential_subpeak_indices) std::fprintf(stderr, " %u", o);
+            std::fprintf(stderr, "\n");
+        }
     for (auto &it : clumps) {
         uint32_t k = it.first;
         for (uint32_t o : it.second.potential_subpeak_indices)

@@ -311,13 +311,13 @@ class Finder:
         return idx, dr2
 
     def stage_times(self) -> np.ndarray:
-        a = np.zeros(16)
-        lib().plan_stage_times(self._h, a.ctypes.data_as(C.POINTER(C.c_double)), 16)
+        a = np.zeros(32)
+        lib().plan_stage_times(self._h, a.ctypes.data_as(C.POINTER(C.c_double)), 32)
         return a
 
     def counters(self) -> np.ndarray:
-        a = np.zeros(16, dtype=np.uint64)
-        lib().plan_counters(self._h, a.ctypes.data_as(C.POINTER(C.c_uint64)), 16)
+        a = np.zeros(32, dtype=np.uint64)
+        lib().plan_counters(self._h, a.ctypes.data_as(C.POINTER(C.c_uint64)), 32)
         return a
 
     def kernel_launches(self) -> int:

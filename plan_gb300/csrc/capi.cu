@@ -238,7 +238,7 @@ int plan_knn(plan_ctx *h, const double *pos3, uint32_t nq, uint32_t k, double es
 
 int plan_stage_times(const plan_ctx *h, double *ms, int n) {
     if (!h || !ms) return kErrArgument;
-    for (int i = 0; i < n && i < 16; ++i) ms[i] = h->c.stage_ms[i];
+    for (int i = 0; i < n && i < 32; ++i) ms[i] = h->c.stage_ms[i];
     return kOk;
 }
 
@@ -246,7 +246,7 @@ uint64_t plan_kernel_launches(const plan_ctx *h) { return h ? h->c.launches : 0;
 
 int plan_counters(const plan_ctx *h, uint64_t *out, int n) {
     if (!h || !out) return kErrArgument;
-    for (int i = 0; i < n && i < 16; ++i) out[i] = h->c.counters[i];
+    for (int i = 0; i < n && i < 32; ++i) out[i] = h->c.counters[i];
     return kOk;
 }
 

@@ -19,8 +19,10 @@
 //  * Hill-sphere rebinding runs clump by clump in key order (the in-clump flags couple
 //    clumps); inside a clump the first bound candidate of each chunk is accepted the same way.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <numeric>
 #include <vector>
 
@@ -106,7 +108,8 @@ __global__ void k_init(uint32_t C, const uint32_t *gkey, const uint32_t *goff, C
 }
 
 // CalculateKinematicProperties (src/tree.hpp:4431-4442): one thread per clump, in order.
-__global__ void k_kinematics(const uint32_t *list, uint32_t n, CT ct, Pool P, const double4_32a *pos, const double4_32a *vel) {
+__global__ void k_kinematics(const uint32_t *list, uint32_t n, CT ct, Pool P, const double4_32a *pos, const double4_32a *vel, int with_hill,
+                             double G, double Omega) {
     uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     uint32_t s = list[t];
@@ -122,6 +125,7 @@ __global__ void k_kinematics(const uint32_t *list, uint32_t n, CT ct, Pool P, co
     ct.M[s] = M;
     ct.com[s] = make_double4_32a(cx / M, cy / M, cz / M, 0);
     ct.vcom[s] = make_double4_32a(vx / M, vy / M, vz / M, 0);
+    if (with_hill) ct.hill[s] = cr_pow_third(M * G / 3. / Omega / Omega);  // src/tree.hpp:4715-4717
 }
 
 // distances to the centre of mass (src/tree.hpp:4448-4450, 4545-4547)
@@ -597,71 +601,176 @@ __global__ void __launch_bounds__(256) k_unbind(const uint32_t *list, CT ct, Poo
     }
 }
 
-// Hill-sphere rebinding of one clump (src/tree.hpp:4678-4711): the ball search's node
-// ranges are walked in order; candidates are evaluated a chunk at a time against the
-// current state and the first bound one is taken.
-__global__ void k_ball_ranges(KTree t, double cx, double cy, double cz, double r, uint32_t *rb, uint32_t *re, uint8_t *rpart, uint32_t cap,
-                              uint32_t *nr, uint32_t *ncand, unsigned *err) {
-    if (threadIdx.x || blockIdx.x) return;
-    uint32_t n = 0, tot = 0;
-    traverse(t, cx, cy, cz, r,
-             [&](uint32_t b, uint32_t e, bool partial) {
-                 if (n < cap) { rb[n] = b; re[n] = e; rpart[n] = partial ? 1 : 0; }
-                 ++n;
-                 tot += e - b;
-                 return true;
-             },
-             err);
-    if (n > cap) atomicOr(err, (unsigned)kDevErrCapacity);
-    *nr = min(n, cap);
-    *ncand = tot;
+// Hill-sphere rebinding (src/tree.hpp:4678-4711). A resumable depth-first walk yields the
+// ball's points in the order of RecursiveBallSearch; one block per clump evaluates them a
+// chunk at a time against the clump's current state and takes the first bound one.
+struct BallWalk {
+    uint32_t node, pos, end;
+    uint8_t partial, done;
+};
+
+__device__ bool ball_walk_advance(const KTree &t, double cx, double cy, double cz, double r, BallWalk &w, unsigned *err) {
+    for (uint32_t guard = 0; guard < 4u * t.nodes + 8u; ++guard) {
+        if (w.done) return false;
+        const uint32_t node = w.node;
+        if (node >= t.nodes) {
+            atomicOr(err, (unsigned)kDevErrBadNode);
+            w.done = 1;
+            return false;
+        }
+        double4_32a nc = t.ncf[node];
+        int visit = 0;
+        bool down = false;
+        if (node_contained(nc, cx, cy, cz, r)) visit = 1;
+        else if (node_intersects(nc, cx, cy, cz, r)) {
+            if (t.nnd[node] == 0) visit = 2;
+            else down = true;
+        }
+        if (down) {
+            w.node = t.nfd[node];
+        } else {
+            uint32_t n2 = node;
+            while (n2 != 0) {
+                uint32_t p = t.npar[n2];
+                if (n2 + 1 < t.nfd[p] + t.nnd[p]) { n2 = n2 + 1; break; }
+                n2 = p;
+            }
+            if (n2 == 0) w.done = 1;
+            w.node = n2;
+        }
+        if (visit) {
+            w.pos = t.nbeg[node];
+            w.end = t.nend[node];
+            w.partial = visit == 2;
+            return true;
+        }
+    }
+    atomicOr(err, (unsigned)kDevErrLoopLimit);
+    w.done = 1;
+    return false;
 }
 
-__global__ void __launch_bounds__(256) k_rebind(uint32_t s, CT ct, Pool P, const double4_32a *pos, const double4_32a *vel, const double *dens,
-                                                uint8_t *in_clump, const uint32_t *rb, const uint32_t *re, const uint8_t *rpart,
-                                                const uint32_t *nr_p, double cx0, double cy0, double cz0, double r, CP cp,
-                                                uint32_t *acc, uint32_t acc_cap, uint32_t *grew, unsigned *err) {
-    __shared__ double sM, scx, scy, scz, svx, svy, svz;
-    __shared__ uint32_t s_nacc, s_first, s_ri, s_rk, s_len, s_noff;
+// One SearchBoundParticlesWithinHillRadius call for every listed clump (one block each).
+// seq_mode = 1: the reference's shared in-clump flags, one clump at a time.
+// seq_mode = 0: clumps run concurrently. owner[q] holds the key rank of the clump holding
+// particle q. A clump treats q as taken if it was marked before rebinding, or is held by
+// itself or by an earlier clump (recording that it deferred, in dmax); it may take q from a
+// later clump, which is then invalid. A clump that loses q to an earlier one is invalid.
+// Invalid clumps are restored and rerun by the host until none is left; the clumps below
+// the lowest invalid rank are final after every pass, so this ends.
+__global__ void __launch_bounds__(256) k_rebind_round(const uint32_t *list, CT ct, Pool P, KTree t, const double4_32a *vel,
+                                                      const double *dens, uint8_t *in_clump, uint32_t *owner, const uint32_t *rank_of,
+                                                      const uint32_t *slot_of_rank, uint8_t *invalid, uint32_t *dmax, int seq_mode, CP cp,
+                                                      uint8_t *grew, uint32_t *mn_out, unsigned *err) {
+    __shared__ double sM, scx, scy, scz, svx, svy, svz, c0x, c0y, c0z, rad;
+    __shared__ uint32_t s_nel, s_first, s_noff, s_len, s_nacc;
+    __shared__ BallWalk w;
     __shared__ uint32_t chunk[256];
     __shared__ uint8_t cpart[256];
-    const uint32_t nr = *nr_p;
+    __shared__ uint32_t warp_cnt[8];
+    const uint32_t slot = list[blockIdx.x];
+    const uint32_t myrank = seq_mode ? 0u : rank_of[slot];
+    const double4_32a *pos = t.pos;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     if (threadIdx.x == 0) {
-        sM = ct.M[s];
-        double4_32a c = ct.com[s], v = ct.vcom[s];
+        sM = ct.M[slot];
+        double4_32a c = ct.com[slot], v = ct.vcom[slot];
         scx = c.x; scy = c.y; scz = c.z;
         svx = v.x; svy = v.y; svz = v.z;
+        c0x = c.x; c0y = c.y; c0z = c.z;  // the ball stays where the call started
+        rad = ct.hill[slot];
+        w = BallWalk{0, 0, 0, 0, 0};
+        s_nel = 0;
         s_nacc = 0;
-        s_ri = 0;
-        s_rk = 0;
     }
     __syncthreads();
-    const double rr = r * r;
-    for (;;) {
-        // the next chunk of candidates in ball-search order (thread 0 walks the ranges)
-        if (threadIdx.x == 0) {
-            uint32_t len = 0, ri = s_ri, rk = s_rk;
-            while (len < blockDim.x && ri < nr) {
-                uint32_t b = rb[ri], e = re[ri];
-                if (b + rk >= e) { ++ri; rk = 0; continue; }
-                chunk[len] = b + rk;
-                cpart[len] = rpart[ri];
-                ++len;
-                ++rk;
+    const double rr = rad * rad;
+    // 0) count the eligible candidates (state-independent tests) to size the segment
+    for (int pass = 0; pass < 2; ++pass) {
+        for (;;) {
+            if (threadIdx.x == 0) {
+                uint32_t len = 0;
+                while (len < blockDim.x) {
+                    if (w.pos < w.end) {
+                        chunk[len] = w.pos;
+                        cpart[len] = w.partial;
+                        ++w.pos;
+                        ++len;
+                    } else if (!ball_walk_advance(t, c0x, c0y, c0z, rad, w, err)) {
+                        break;
+                    }
+                }
+                s_len = len;
             }
-            s_len = len;
-            s_first = kNone;
+            __syncthreads();
+            const uint32_t len = s_len;
+            if (len == 0) break;
+            bool keep = false;
+            uint32_t q = 0;
+            if (threadIdx.x < len) {
+                q = chunk[threadIdx.x];
+                const double4_32a p = pos[q];
+                // RecursiveBallSearch keeps leaf points within r; contained nodes pass whole
+                bool inside = !cpart[threadIdx.x] || point_dr2(c0x, c0y, c0z, p) <= rr;
+                keep = inside && in_clump[q] == 0 && !(dens[q] < cp.thr);
+                if (keep && !seq_mode) {
+                    uint32_t ow = owner[q];
+                    if (ow != kNone && ow <= myrank) {  // held by this or an earlier clump
+                        keep = false;
+                        if (ow < myrank && pass == 1) atomicMax(&dmax[slot], ow + 1);
+                    }
+                }
+            }
+            unsigned bal = __ballot_sync(0xffffffffu, keep);
+            if (lane == 0) warp_cnt[wid] = __popc(bal);
+            __syncthreads();
+            if (pass == 1) {
+                uint32_t before = 0;
+                for (int k = 0; k < wid; ++k) before += warp_cnt[k];
+                if (keep) P.idx[s_noff + ct.mn[slot] + s_nel + before + __popc(bal & ((1u << lane) - 1u))] = q;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                uint32_t tot = 0;
+                for (int k = 0; k < (int)(blockDim.x / 32); ++k) tot += warp_cnt[k];
+                s_nel += tot;
+            }
+            __syncthreads();
         }
+        if (pass == 0) {
+            // segment: the members, the eligible candidates in walk order, then the accepted
+            // ones (at most one per eligible candidate)
+            if (threadIdx.x == 0) {
+                s_noff = pool_alloc(P, ct.mn[slot] + 2 * s_nel, err);
+                w = BallWalk{0, 0, 0, 0, 0};
+                s_nel = 0;
+            }
+            __syncthreads();
+            if (s_noff == kNone) return;
+        }
+    }
+    const uint32_t m0 = ct.mn[slot], o = ct.moff[slot], no = s_noff;
+    for (uint32_t k = threadIdx.x; k < m0; k += blockDim.x) P.idx[no + k] = P.idx[o + k];
+    uint32_t *elig = P.idx + no + m0;  // eligible candidates in walk order
+    // 2) the reference's sequential acceptance over the eligible candidates, a chunk at a time
+    const uint32_t nel = s_nel;
+    uint32_t *acc = elig + nel;  // accepted, in acceptance order
+    uint32_t at = 0;
+    while (at < nel) {
+        if (threadIdx.x == 0) s_first = kNone;
         __syncthreads();
-        const uint32_t len = s_len;
-        if (len == 0) break;
+        uint32_t k = at + threadIdx.x;
         bool bound = false;
-        if (threadIdx.x < len) {
-            uint32_t q = chunk[threadIdx.x];
-            double4_32a p = pos[q], v = vel[q];
-            // RecursiveBallSearch keeps leaf points within r (contained nodes pass whole)
-            bool inside = !cpart[threadIdx.x] || point_dr2(cx0, cy0, cz0, p) <= rr;
-            if (inside && !in_clump[q] && !(dens[q] < cp.thr)) {
+        if (k < nel) {
+            const uint32_t q2 = elig[k];
+            bool taken = seq_mode && in_clump[q2] != 0;
+            if (!taken && !seq_mode) {
+                uint32_t ow = owner[q2];
+                taken = ow != kNone && ow <= myrank;
+                if (ow != kNone && ow < myrank) atomicMax(&dmax[slot], ow + 1);
+            }
+            if (!taken) {
+                const double4_32a p = pos[q2], v = vel[q2];
                 double M = sM + p.w;
                 double dx = scx - p.x;
                 double ex = (svx - 0.0 * dx) - v.x, ey = (svy - cp.shear * dx) - v.y, ez = (svz - 0.0 * dx) - v.z;
@@ -671,54 +780,83 @@ __global__ void __launch_bounds__(256) k_rebind(uint32_t s, CT ct, Pool P, const
         }
         if (bound) atomicMin(&s_first, threadIdx.x);
         __syncthreads();
-        if (threadIdx.x == 0) {
-            const uint32_t f = s_first;
-            const uint32_t adv = (f == kNone) ? len : f + 1;
-            if (f != kNone) {  // take it and update the state (src/tree.hpp:4696-4701)
-                uint32_t q = chunk[f];
-                double4_32a p = pos[q], v = vel[q];
-                double M = sM + p.w;
-                scx = (scx * M + p.w * p.x) / M; scy = (scy * M + p.w * p.y) / M; scz = (scz * M + p.w * p.z) / M;
-                svx = (M * svx + p.w * v.x) / M; svy = (M * svy + p.w * v.y) / M; svz = (M * svz + p.w * v.z) / M;
-                sM = M;
-                in_clump[q] = 1;
-                if (s_nacc < acc_cap) acc[s_nacc] = q;
-                else atomicOr(err, (unsigned)kDevErrCapacity);
-                s_nacc = s_nacc + 1;
+        const uint32_t f = s_first;
+        if (f == kNone) {
+            at += blockDim.x;
+            continue;
+        }
+        if (threadIdx.x == 0) {  // take it and update the state (src/tree.hpp:4696-4701)
+            const uint32_t q2 = elig[at + f];
+            const double4_32a p = pos[q2], v = vel[q2];
+            double M = sM + p.w;
+            scx = (scx * M + p.w * p.x) / M; scy = (scy * M + p.w * p.y) / M; scz = (scz * M + p.w * p.z) / M;
+            svx = (M * svx + p.w * v.x) / M; svy = (M * svy + p.w * v.y) / M; svz = (M * svz + p.w * v.z) / M;
+            sM = M;
+            if (seq_mode) {
+                in_clump[q2] = 1;
+            } else {
+                uint32_t old = atomicMin(&owner[q2], myrank);
+                if (old != kNone && old > myrank) invalid[slot_of_rank[old]] = 1;  // taken from a later clump
+                if (old != kNone && old < myrank) invalid[slot] = 1;               // an earlier clump got it first
             }
-            uint32_t ri = s_ri, rk = s_rk, left = adv;
-            while (left > 0 && ri < nr) {
-                uint32_t b = rb[ri], e = re[ri];
-                uint32_t avail = (b + rk < e) ? e - (b + rk) : 0;
-                if (avail == 0) { ++ri; rk = 0; continue; }
-                uint32_t take = min(avail, left);
-                rk += take;
-                left -= take;
-            }
-            s_ri = ri;
-            s_rk = rk;
+            acc[s_nacc] = q2;
+            s_nacc = s_nacc + 1;
         }
         __syncthreads();
+        at += f + 1;
     }
-    // new segment: previous members in order, then the accepted ones in acceptance order
-    const uint32_t nacc = min(s_nacc, acc_cap), m0 = ct.mn[s], o = ct.moff[s];
-    if (threadIdx.x == 0) s_noff = nacc ? pool_alloc(P, m0 + nacc, err) : o;
     __syncthreads();
-    const uint32_t no = s_noff;
-    if (no == kNone) return;
-    if (nacc) {
-        for (uint32_t k = threadIdx.x; k < m0; k += blockDim.x) P.idx[no + k] = P.idx[o + k];
-        for (uint32_t k = threadIdx.x; k < nacc; k += blockDim.x) P.idx[no + m0 + k] = acc[k];
-    }
+    const uint32_t nacc = s_nacc;
+    // members followed by the accepted ones (indices order of the reference)
+    for (uint32_t k = threadIdx.x; k < nacc; k += blockDim.x) P.idx[no + m0 + k] = acc[k];
     __syncthreads();
     if (threadIdx.x == 0) {
-        *grew = nacc ? 1u : 0u;
-        ct.moff[s] = no;
-        ct.mn[s] = m0 + nacc;
-        ct.M[s] = sM;
-        ct.com[s] = make_double4_32a(scx, scy, scz, 0);
-        ct.vcom[s] = make_double4_32a(svx, svy, svz, 0);
+        grew[blockIdx.x] = nacc ? 1 : 0;
+        mn_out[blockIdx.x] = m0 + nacc;
+        if (nacc) {
+            ct.moff[slot] = no;
+            ct.mn[slot] = m0 + nacc;
+            ct.M[slot] = sM;
+            ct.com[slot] = make_double4_32a(scx, scy, scz, 0);
+            ct.vcom[slot] = make_double4_32a(svx, svy, svz, 0);
+        }
     }
+}
+
+// restore listed clumps to their state before rebinding (segments re-materialised from the
+// saved pool) and clear their per-pass records
+__global__ void k_rebind_restore(const uint32_t *list, uint32_t n, CT ct, Pool P, const double *bM, const double *bh, const double *bri,
+                                 const double *bro, const double *br10, const double *br2, const double4_32a *bc, const double4_32a *bv,
+                                 const uint32_t *bo, const uint32_t *bn, const uint32_t *bidx, const double *bdist, uint8_t *invalid,
+                                 uint32_t *dmax, unsigned *err) {
+    __shared__ uint32_t s_off;
+    uint32_t t = blockIdx.x;
+    if (t >= n) return;
+    uint32_t sl = list[t];
+    if (threadIdx.x == 0) {
+        ct.M[sl] = bM[sl]; ct.hill[sl] = bh[sl]; ct.r_in[sl] = bri[sl]; ct.r_out[sl] = bro[sl]; ct.r10[sl] = br10[sl]; ct.r2s[sl] = br2[sl];
+        ct.com[sl] = bc[sl]; ct.vcom[sl] = bv[sl];
+        s_off = pool_alloc(P, bn[sl], err);
+        invalid[sl] = 0;
+        dmax[sl] = 0;
+    }
+    __syncthreads();
+    if (s_off == kNone) return;
+    for (uint32_t k = threadIdx.x; k < bn[sl]; k += blockDim.x) {
+        P.idx[s_off + k] = bidx[bo[sl] + k];
+        P.dist[s_off + k] = bdist[bo[sl] + k];
+    }
+    if (threadIdx.x == 0) {
+        ct.moff[sl] = s_off;
+        ct.mn[sl] = bn[sl];
+    }
+}
+
+__global__ void k_rebind_release(uint32_t Tu, uint32_t *owner, const uint8_t *rerun_rank) {
+    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= Tu) return;
+    uint32_t o = owner[q];
+    if (o != kNone && rerun_rank[o]) owner[q] = kNone;
 }
 
 __global__ void k_mark_members(uint32_t C, CT ct, Pool P, uint8_t *in_clump) {
@@ -785,6 +923,22 @@ __global__ void k_angmom(const uint32_t *list, uint32_t n, CT ct, Pool P, const 
     ct.J[s] = make_double4_32a(jx, jy, jz, 0);
 }
 
+// copy every live segment into the other pool buffer at packed offsets
+__global__ void k_compact(uint32_t C, CT ct, Pool P, const uint32_t *newoff, uint32_t *dst_idx, double *dst_dist) {
+    uint32_t s = blockIdx.x;
+    if (s >= C || !ct.alive[s]) return;
+    const uint32_t o = ct.moff[s], m = ct.mn[s], no = newoff[s];
+    for (uint32_t k = threadIdx.x; k < m; k += blockDim.x) {
+        dst_idx[no + k] = P.idx[o + k];
+        dst_dist[no + k] = P.dist[o + k];
+    }
+}
+
+__global__ void k_set_offsets(uint32_t C, CT ct, const uint32_t *newoff) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < C && ct.alive[s]) ct.moff[s] = newoff[s];
+}
+
 // output gather: per final clump member (particles order): tree index -> pos/vel/orig,
 // and the number of offset sources (sink particles expand)
 __global__ void k_out_counts(const uint32_t *list, uint32_t nl, const uint32_t *base, CT ct, Pool P, const uint32_t *sink_n,
@@ -835,6 +989,9 @@ struct Stage {
     CP cp;
     uint32_t C = 0;
     uint32_t *slot_of_key = nullptr;
+    uint32_t *alt_idx = nullptr;  // second pool buffer for compaction
+    double *alt_dist = nullptr;
+    uint32_t *d_off = nullptr;
     uint32_t *d_list = nullptr;   // scratch slot list (capacity C)
     uint32_t *d_list2 = nullptr;
     uint8_t *d_flag8 = nullptr;
@@ -871,18 +1028,20 @@ struct Stage {
         return kOk;
     }
 
-    int kinematics(const std::vector<uint32_t> &list) {
+    int kinematics(const std::vector<uint32_t> &list, bool with_hill = false) {
         if (list.empty()) return kOk;
         int rc = up_list(list, d_list);
         if (rc) return rc;
-        k_kinematics<<<grid_for(list.size(), 64), 64, 0, s>>>(d_list, (uint32_t)list.size(), ct, P, tr.pos, tr.vel);
+        k_kinematics<<<grid_for(list.size(), 64), 64, 0, s>>>(d_list, (uint32_t)list.size(), ct, P, tr.pos, tr.vel, with_hill ? 1 : 0, cp.G,
+                                                               cp.Omega);
         c.launches++;
         PLAN_CUDA(cudaGetLastError());
         return kOk;
     }
 
     // distances, sort, radii for the listed clumps (the tail of SortParticles / Merge)
-    int resort(const std::vector<uint32_t> &list) {
+    // known_mn: sizes of the listed clumps when the caller has them (saves a download)
+    int resort(const std::vector<uint32_t> &list, bool radii = true, const std::vector<uint32_t> *known_mn = nullptr) {
         if (list.empty()) return kOk;
         int rc = up_list(list, d_list);
         if (rc) return rc;
@@ -891,13 +1050,18 @@ struct Stage {
         k_sort_small<<<n, 1024, 0, s>>>(d_list, ct, P);
         c.launches += 2;
         // segments longer than the in-block sort go through the radix sort
-        std::vector<uint32_t> mn;
-        rc = down(mn, ct.mn, C);
-        if (rc) return rc;
+        std::vector<uint32_t> mn_all, mn_list;
+        if (known_mn) {
+            mn_list = *known_mn;
+        } else {
+            rc = down(mn_all, ct.mn, C);
+            if (rc) return rc;
+            for (uint32_t sl : list) mn_list.push_back(mn_all[sl]);
+        }
         std::vector<uint32_t> large, base;
         uint64_t tot = 0;
-        for (uint32_t sl : list)
-            if (mn[sl] > (uint32_t)kSmallSort) { large.push_back(sl); base.push_back((uint32_t)tot); tot += mn[sl]; }
+        for (size_t k = 0; k < list.size(); ++k)
+            if (mn_list[k] > (uint32_t)kSmallSort) { large.push_back(list[k]); base.push_back((uint32_t)tot); tot += mn_list[k]; }
         if (!large.empty()) {
             Arena &S = c.scratch;
             size_t mark = S.used;
@@ -920,15 +1084,20 @@ struct Stage {
             rc = up_list(list, d_list);
             if (rc) return rc;
         }
-        k_one10th<<<n, 256, 0, s>>>(d_list, ct, P, tr.pos, tr.dens);
-        c.launches++;
+        if (radii) {
+            k_one10th<<<n, 256, 0, s>>>(d_list, ct, P, tr.pos, tr.dens);
+            c.launches++;
+        }
         PLAN_CUDA(cudaGetLastError());
         return kOk;
     }
 
-    int sort_particles(const std::vector<uint32_t> &list) {
-        int rc = kinematics(list);
-        if (!rc) rc = resort(list);
+    // SortParticles; the one-tenth radii are only read by the merge sweeps, and with_hill
+    // folds the CalculateHillRadius that follows every later SortParticles into the sums
+    int sort_particles(const std::vector<uint32_t> &list, bool radii = true, bool with_hill = false,
+                       const std::vector<uint32_t> *known_mn = nullptr) {
+        int rc = kinematics(list, with_hill);
+        if (!rc) rc = resort(list, radii, known_mn);
         return rc;
     }
 
@@ -952,6 +1121,36 @@ struct Stage {
         return kOk;
     }
 
+    // Pack the live segments into the other buffer once the bump allocator has used half
+    // of the pool (merges and rebinding write fresh segments and abandon the old ones).
+    int maybe_compact(bool force = false) {
+        uint32_t top = 0;
+        PLAN_CUDA(cudaMemcpyAsync(&top, P.top, 4, cudaMemcpyDeviceToHost, s));
+        int rc = sync();
+        if (rc) return rc;
+        if (!force && top < P.cap / 2) return kOk;
+        std::vector<uint32_t> mn;
+        std::vector<uint8_t> alive;
+        rc = down(mn, ct.mn, C);
+        if (!rc) rc = down(alive, ct.alive, C);
+        if (rc) return rc;
+        std::vector<uint32_t> off(C + 1, 0);
+        uint64_t run = 0;
+        for (uint32_t i = 0; i < C; ++i) { off[i] = (uint32_t)run; if (alive[i]) run += mn[i]; }
+        if (run > P.cap) return kErrDeviceLimit;
+        PLAN_CUDA(cudaMemcpyAsync(d_off, off.data(), (size_t)C * 4, cudaMemcpyHostToDevice, s));
+        k_compact<<<C, 256, 0, s>>>(C, ct, P, d_off, alt_idx, alt_dist);
+        k_set_offsets<<<grid_for(C, 256), 256, 0, s>>>(C, ct, d_off);
+        c.launches += 2;
+        std::swap(P.idx, alt_idx);
+        std::swap(P.dist, alt_dist);
+        uint32_t t32 = (uint32_t)run;
+        PLAN_CUDA(cudaMemcpyAsync(P.top, &t32, 4, cudaMemcpyHostToDevice, s));
+        ++compactions;
+        return sync();
+    }
+    uint32_t compactions = 0;
+
     int unbind(const std::vector<uint32_t> &list) {
         if (list.empty()) return kOk;
         int rc = up_list(list, d_list);
@@ -959,11 +1158,17 @@ struct Stage {
         k_unbind<<<(unsigned)list.size(), 256, 0, s>>>(d_list, ct, P, tr.pos, tr.vel, cp);
         c.launches++;
         PLAN_CUDA(cudaGetLastError());
-        return sort_particles(list);  // RemoveUnboundParticles ends with SortParticles
+        // RemoveUnboundParticles ends with SortParticles; every caller computes the Hill
+        // radius right after it (src/tree.hpp:4190-4191, 4241-4242)
+        return sort_particles(list, false, true);
     }
 };
 
 }  // namespace
+
+static double wall_ms() {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
 
 int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogue **out) {
     cudaEvent_t ev[6];
@@ -1032,9 +1237,12 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
     ct.sub_head = A.get<uint32_t>(C + 1); ct.sub_tail = A.get<uint32_t>(C + 1);
     Pool &P = st.P;
     const uint32_t m0 = hg.n_members;
-    P.cap = (uint32_t)std::min<uint64_t>(0xfffffff0ull, 4ull * m0 + Tu / 2 + 4096);
+    P.cap = (uint32_t)std::min<uint64_t>(0xfffffff0ull, 3ull * m0 + Tu / 4 + 4096);
     P.idx = A.get<uint32_t>(P.cap);
     P.dist = A.get<double>(P.cap);
+    st.alt_idx = A.get<uint32_t>(P.cap);
+    st.alt_dist = A.get<double>(P.cap);
+    st.d_off = A.get<uint32_t>(C + 1);
     P.top = A.get<uint32_t>(4);
     P.sub_cap = C + 16;
     P.sub_peak = A.get<uint32_t>(P.sub_cap);
@@ -1059,6 +1267,9 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
     }
     c.counters[5] = m0;
     c.counters[6] = C;
+    PLAN_CUDA(cudaStreamSynchronize(s));
+    double tw0 = wall_ms();
+    for (int k = 15; k < 32; ++k) c.stage_ms[k] = 0;
     std::vector<uint32_t> all(C);
     std::iota(all.begin(), all.end(), 0u);
     // SortParticles + the diffuse cut after HOP (src/tree.hpp:3816-3829)
@@ -1162,7 +1373,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                     for (uint32_t k = 0; k < hcnt[sl]; ++k) cp1[hoff[sl] + k] = sl;
                 PLAN_CUDA(cudaMemcpyAsync(d_cp1, cp1.data(), (size_t)ncand * 4, cudaMemcpyHostToDevice, s));
                 PLAN_CUDA(cudaMemsetAsync(st.d_u + 16, 0, 4, s));
-                k_pair_eval<<<grid_for(ncand, 128), 128, 0, s>>>(ncand, d_cp1, d_cand, ctree.in_vel, ct, st.slot_of_key, st.cp, hill_mode,
+                k_pair_eval<<<grid_for(ncand, 128), 128, 0, s>>>(ncand, d_cp1, d_cand, ctree.vel, ct, st.slot_of_key, st.cp, hill_mode,
                                                                  d_code, d_p2, d_sq, d_sest, d_sof, st.d_u + 16);
                 PLAN_CUDA(cudaMemcpyAsync(&nsaddle, st.d_u + 16, 4, cudaMemcpyDeviceToHost, s));
                 rc = st.sync();
@@ -1185,6 +1396,13 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
             if (rc) return rc;
             const uint32_t npairs = h_u[1];
             delete_count = h_u[0];
+            if (std::getenv("PLAN_DEBUG_MERGES") && npairs) {
+                std::vector<uint32_t> hp, hk;
+                rc = st.down(hp, d_pairs, 2 * (size_t)npairs);
+                if (!rc) rc = st.down(hk, ct.key, C);
+                if (rc) return rc;
+                for (uint32_t k = 0; k < npairs; ++k) std::fprintf(stderr, "merge kind %d pred %u prey %u\n", kind, hk[hp[2 * k]], hk[hp[2 * k + 1]]);
+            }
             merged_any = npairs > 0;
             if (npairs) {
                 PLAN_CUDA(cudaMemsetAsync(d_wave, 0xff, (size_t)(C + 1) * 4, s));
@@ -1196,6 +1414,8 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                 c.launches++;
                 const uint32_t npred = hw[0], nwaves = hw[1];
                 for (uint32_t w = 0; w < nwaves; ++w) {
+                    rc = st.maybe_compact();
+                    if (rc) return rc;
                     PLAN_CUDA(cudaMemsetAsync(st.d_u + 24, 0, 4, s));
                     k_merge<<<npred, 256, 0, s>>>(npred, d_pl, d_pf, d_pc, d_pw, w, d_pairs, ct, P, tr.dens, d_merged, st.d_u + 24, c.d_err);
                     c.launches++;
@@ -1236,6 +1456,8 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
             }
             num_planetesimals = (uint32_t)live.size() - delete_count;
             (hill_mode ? c.counters[12] : c.counters[11])++;
+            rc = st.maybe_compact();
+            if (rc) return rc;
         }
         // erase the deleted clumps (and a clump keyed 0 when the zero-filled list has room,
         // src/tree.hpp:3874, 4000-4002)
@@ -1262,11 +1484,26 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
         // all survivors are masked again by construction (every unmasked clump was deleted)
     }
     A.used = arena_mark;
+    double tw1 = wall_ms();
     c.counters[13] = quirk;
     c.counters[14] = nunknown_total;
     cudaEventRecord(ev[4], s);
 
     // re-key (src/tree.hpp:4156-4182)
+    if (std::getenv("PLAN_DEBUG_MERGES")) {
+        std::vector<uint32_t> hk, hpk, hh, hsp, hsn;
+        rc = st.down(hk, ct.key, C);
+        if (!rc) rc = st.down(hpk, ct.peak, C);
+        if (!rc) rc = st.down(hh, ct.sub_head, C);
+        if (!rc) rc = st.down(hsp, P.sub_peak, P.sub_cap);
+        if (!rc) rc = st.down(hsn, P.sub_next, P.sub_cap);
+        if (rc) return rc;
+        for (uint32_t sl : live) {
+            std::fprintf(stderr, "clump %u peak %u subs", hk[sl], hpk[sl]);
+            for (uint32_t e = hh[sl]; e != kNone; e = hsn[e]) std::fprintf(stderr, " %u", hsp[e]);
+            std::fprintf(stderr, "\n");
+        }
+    }
     if (!live.empty()) {
         int rc2 = st.up_list(live, st.d_list2);
         if (rc2) return rc2;
@@ -1276,46 +1513,137 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
         if (rc) return rc;
     }
     // 5. unbind, mark, rebind (src/tree.hpp:4189-4208)
-    rc = st.unbind(live);
-    if (!rc) rc = st.hill(live);
+    rc = st.unbind(live);  // includes SortParticles and the Hill radius
     if (rc) return rc;
+    PLAN_CUDA(cudaStreamSynchronize(s));
+    double tw2 = wall_ms();
     PLAN_CUDA(cudaMemsetAsync(in_clump, 0, Tu, s));
     if (C) {
         k_mark_members<<<C, 256, 0, s>>>(C, ct, P, in_clump);
         c.launches++;
     }
     {
-        const uint32_t rcap = 1u << 20;
-        const uint32_t acc_cap = Tu;
-        uint32_t *rb = A.get<uint32_t>(rcap), *re = A.get<uint32_t>(rcap), *acc = A.get<uint32_t>(acc_cap);
-        uint8_t *rpart = A.get<uint8_t>(rcap);
+        // Clumps rebind concurrently (one SearchBound call per clump per round) under the
+        // ordered-claim rule of k_rebind_round; passes rerun invalid clumps from their saved
+        // state until the result equals the reference's clump-by-clump run in key order.
+        const size_t nb = (size_t)C + 1;
+        double *bM = A.get<double>(nb), *bh = A.get<double>(nb), *bri = A.get<double>(nb), *bro = A.get<double>(nb);
+        double *br10 = A.get<double>(nb), *br2 = A.get<double>(nb);
+        double4_32a *bc = A.get<double4_32a>(nb), *bv = A.get<double4_32a>(nb);
+        uint32_t *bo = A.get<uint32_t>(nb), *bn = A.get<uint32_t>(nb), *owner = A.get<uint32_t>(Tu);
+        uint32_t *rank_of = A.get<uint32_t>(nb), *slot_of_rank = A.get<uint32_t>(nb), *dmax = A.get<uint32_t>(nb);
+        uint8_t *d_grew = A.get<uint8_t>(nb), *invalid = A.get<uint8_t>(nb), *rerun_rank = A.get<uint8_t>(nb);
+        uint32_t *d_mnout = A.get<uint32_t>(nb);
         if (A.failed) return kErrOutOfMemory;
-        KTree kt = ktree_of(tr);
-        std::vector<double4_32a> com1(1);
-        std::vector<double> h1(1);
-        for (uint32_t sl : live) {
-            for (int iter = 0; iter < 100000; ++iter) {
-                rc = st.down(com1, ct.com + sl, 1);
-                if (!rc) rc = st.down(h1, ct.hill + sl, 1);
-                if (rc) return rc;
-                k_ball_ranges<<<1, 1, 0, s>>>(kt, com1[0].x, com1[0].y, com1[0].z, h1[0], rb, re, rpart, rcap, st.d_u + 40, st.d_u + 41, c.d_err);
-                k_rebind<<<1, 256, 0, s>>>(sl, ct, P, tr.pos, tr.vel, tr.dens, in_clump, rb, re, rpart, st.d_u + 40, com1[0].x, com1[0].y,
-                                           com1[0].z, h1[0], st.cp, acc, acc_cap, st.d_u + 42, c.d_err);
-                c.launches += 2;
-                std::vector<uint32_t> g;
-                rc = st.down(g, st.d_u + 42, 1);
-                if (rc) return rc;
-                std::vector<uint32_t> one{sl};
-                if (g[0]) {
-                    rc = st.sort_particles(one);
-                    if (rc) return rc;
-                }
-                rc = st.hill(one);
-                if (rc) return rc;
-                if (!g[0]) break;
-            }
+        const uint32_t nlive = (uint32_t)live.size();
+        // save the state (the member pool is packed first, then copied aside)
+        uint32_t saved_top = 0;
+        uint32_t *bidx = nullptr;
+        double *bdist = nullptr;
+        if (nlive) {
+            rc = st.maybe_compact(true);
+            if (rc) return rc;
+            auto cp8 = [&](void *dst, const void *src, size_t b) -> int {
+                PLAN_CUDA(cudaMemcpyAsync(dst, src, b, cudaMemcpyDeviceToDevice, s));
+                return kOk;
+            };
+            rc = cp8(bM, ct.M, C * 8) | cp8(bh, ct.hill, C * 8) | cp8(bri, ct.r_in, C * 8) | cp8(bro, ct.r_out, C * 8) |
+                 cp8(br10, ct.r10, C * 8) | cp8(br2, ct.r2s, C * 8) | cp8(bc, ct.com, C * 32) | cp8(bv, ct.vcom, C * 32) |
+                 cp8(bo, ct.moff, C * 4) | cp8(bn, ct.mn, C * 4);
+            if (rc) return kErrDevice;
+            PLAN_CUDA(cudaMemcpyAsync(&saved_top, P.top, 4, cudaMemcpyDeviceToHost, s));
+            rc = st.sync();
+            if (rc) return rc;
+            bidx = A.get<uint32_t>(saved_top + 1);
+            bdist = A.get<double>(saved_top + 1);
+            if (A.failed) return kErrOutOfMemory;
+            PLAN_CUDA(cudaMemcpyAsync(bidx, P.idx, (size_t)saved_top * 4, cudaMemcpyDeviceToDevice, s));
+            PLAN_CUDA(cudaMemcpyAsync(bdist, P.dist, (size_t)saved_top * 8, cudaMemcpyDeviceToDevice, s));
         }
+        std::vector<uint32_t> h_rank(C, kNone);
+        for (uint32_t r = 0; r < nlive; ++r) h_rank[live[r]] = r;
+        PLAN_CUDA(cudaMemcpyAsync(rank_of, h_rank.data(), (size_t)C * 4, cudaMemcpyHostToDevice, s));
+        PLAN_CUDA(cudaMemcpyAsync(slot_of_rank, live.data(), (size_t)nlive * 4, cudaMemcpyHostToDevice, s));
+        PLAN_CUDA(cudaMemsetAsync(owner, 0xff, (size_t)Tu * 4, s));
+        PLAN_CUDA(cudaMemsetAsync(invalid, 0, nb, s));
+        PLAN_CUDA(cudaMemsetAsync(dmax, 0, nb * 4, s));
+        KTree kt = ktree_of(tr);
+        uint64_t rounds = 0, passes = 0, reruns = 0;
+        auto run_rounds = [&](std::vector<uint32_t> active, int seq_mode) -> int {
+            for (int round = 0; !active.empty(); ++round) {
+                if (round > 200000) return kErrDeviceLimit;
+                ++rounds;
+                int r = st.up_list(active, st.d_list);
+                if (r) return r;
+                double t_a = wall_ms();
+                k_rebind_round<<<(unsigned)active.size(), 256, 0, s>>>(st.d_list, ct, P, kt, tr.vel, tr.dens, in_clump, owner, rank_of,
+                                                                       slot_of_rank, invalid, dmax, seq_mode, st.cp, d_grew, d_mnout, c.d_err);
+                c.launches++;
+                PLAN_CUDA(cudaGetLastError());
+                std::vector<uint8_t> g;
+                std::vector<uint32_t> mo;
+                r = st.down(g, d_grew, active.size());
+                if (!r) r = st.down(mo, d_mnout, active.size());
+                if (r) return r;
+                double t_b = wall_ms();
+                c.stage_ms[16] += t_b - t_a;
+                std::vector<uint32_t> grown, grown_mn;
+                for (size_t k = 0; k < active.size(); ++k)
+                    if (g[k]) { grown.push_back(active[k]); grown_mn.push_back(mo[k]); }
+                // SortParticles when the clump grew, then CalculateHillRadius (unchanged mass
+                // gives an unchanged radius for the others)
+                r = st.sort_particles(grown, false, true, &grown_mn);
+                if (!r) r = st.sync();
+                double t_c = wall_ms();
+                c.stage_ms[17] += t_c - t_b;
+                if (!r) r = st.maybe_compact();
+                if (r) return r;
+                c.stage_ms[18] += wall_ms() - t_c;
+                uint64_t mx = 0;
+                for (uint32_t v : grown_mn) mx = std::max<uint64_t>(mx, v);
+                c.counters[16] = std::max<uint64_t>(c.counters[16], mx);
+                active.swap(grown);
+            }
+            return kOk;
+        };
+        std::vector<uint32_t> active = live;
+        for (uint32_t pass = 0; !active.empty(); ++pass) {
+            if (pass > nlive + 2) return kErrDeviceLimit;
+            ++passes;
+            rc = run_rounds(active, 0);
+            if (rc) return rc;
+            std::vector<uint8_t> inv;
+            std::vector<uint32_t> dm;
+            rc = st.down(inv, invalid, C);
+            if (!rc) rc = st.down(dm, dmax, C);
+            if (rc) return rc;
+            uint32_t rstar = kNone;
+            for (uint32_t r = 0; r < nlive; ++r) if (inv[live[r]]) { rstar = r; break; }
+            if (rstar == kNone) break;
+            std::vector<uint32_t> rerun;
+            std::vector<uint8_t> rr(nlive + 1, 0);
+            for (uint32_t r = rstar; r < nlive; ++r) {
+                uint32_t sl = live[r];
+                if (inv[sl] || (dm[sl] && dm[sl] - 1 >= rstar)) { rerun.push_back(sl); rr[r] = 1; }
+            }
+            reruns += rerun.size();
+            PLAN_CUDA(cudaMemcpyAsync(rerun_rank, rr.data(), nlive, cudaMemcpyHostToDevice, s));
+            k_rebind_release<<<grid_for(Tu, 256), 256, 0, s>>>(Tu, owner, rerun_rank);
+            rc = st.up_list(rerun, st.d_list2);
+            if (rc) return rc;
+            k_rebind_restore<<<(unsigned)rerun.size(), 256, 0, s>>>(st.d_list2, (uint32_t)rerun.size(), ct, P, bM, bh, bri, bro, br10, br2,
+                                                                    bc, bv, bo, bn, bidx, bdist, invalid, dmax, c.d_err);
+            c.launches += 2;
+            PLAN_CUDA(cudaGetLastError());
+            active = rerun;
+        }
+        // final ownership = the reference's in-clump marks of rebinding
+        c.stage_ms[14] = (double)rounds;
+        c.counters[14] = reruns;
+        c.counters[12] = passes;
     }
+    PLAN_CUDA(cudaStreamSynchronize(s));
+    double tw3 = wall_ms();
     // 6. prune and loose streams (src/tree.hpp:4213-4224)
     auto prune = [&]() -> int {
         if (!C) return kOk;
@@ -1359,8 +1687,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
             rc = st.down(changed, st.d_list2, nch[0]);
             if (rc) return rc;
             rc = st.kinematics(changed);
-            if (!rc) rc = st.unbind(changed);
-            if (!rc) rc = st.hill(changed);
+            if (!rc) rc = st.unbind(changed);  // includes SortParticles and the Hill radius
             if (rc) return rc;
         }
         rc = st.live_order(live);
@@ -1393,6 +1720,13 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
         c.launches++;
     }
     cudaEventRecord(ev[5], s);
+    PLAN_CUDA(cudaStreamSynchronize(s));
+    double tw4 = wall_ms();
+    c.stage_ms[10] = tw1 - tw0;  // HOP-group sort + both merge sweeps
+    c.stage_ms[11] = tw2 - tw1;  // re-key + unbinding
+    c.stage_ms[12] = tw3 - tw2;  // Hill rebinding
+    c.stage_ms[13] = tw4 - tw3;  // prune, rip, ghost cut, J
+    c.counters[15] = st.compactions;
 
     // ------------------------------------------------------------------ catalogue
     plan_catalogue *cat = new plan_catalogue();
@@ -1477,6 +1811,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
     cudaEventElapsedTime(&ms, ev[1], ev[2]); c.stage_ms[5] = ms;
     cudaEventElapsedTime(&ms, ev[2], ev[3]); c.stage_ms[6] = ms;
     cudaEventElapsedTime(&ms, ev[3], ev[5]); c.stage_ms[7] = ms;
+    c.stage_ms[8] = wall_ms() - tw4;  // catalogue download and host finishing
     for (auto &e : ev) cudaEventDestroy(e);
     c.counters[7] = cat->clumps.size();
     if (out) *out = cat;

@@ -75,8 +75,8 @@ struct Context {
     DevTree tree;
     unsigned *d_err = nullptr;      // device error flags
     uint64_t launches = 0;
-    double stage_ms[16] = {0};
-    uint64_t counters[16] = {0};
+    double stage_ms[32] = {0};
+    uint64_t counters[32] = {0};
     std::string last_error;
     // host copies kept for the catalogue
     uint32_t n_input = 0;
