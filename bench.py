@@ -1,0 +1,367 @@
+#!/usr/bin/env python3
+"""Throughput of the clump-finding path (BuildTree + FindPlanetesimals) on one GB300.
+
+A step is one snapshot through the whole path: ingest of the 44-byte .lis records, ghosts,
+Morton keys, radix sort, sinks, octree, KNN densities, densest neighbours, HOP groups and
+the clump stage down to the host catalogue. The workload is the 16,777,216-particle
+snapshot (60% uniform, 25% in four Gaussian sheets, 15% in 200 Plummer clumps with a
+M^-1.6 mass function, 10% of them unbound), generated in memory from a fixed seed.
+
+  value  particles/s with the records already in device memory when the timer starts;
+  e2e    particles/s through the same C-ABI call with page-locked HOST records, so the
+         host-to-device copy of the records and the read-back of the catalogue are inside
+         the timed region.
+
+Several GPUs run independent replicas (one snapshot per rank, no collective on the data
+path); value is the particles of all ranks over the slowest rank's time.
+
+`--impl reference` times the CPU restatement of the same path (oracle/, the reference's
+algorithm; the reference program itself is not built where this runs) with all host
+cores on a bounded sample of the same workload, and prints the same JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOAD = 2
+N_FULL = 1 << 24
+SEED = 1
+NX = 128
+KNN, HOP = 32, 16
+WORKLOAD_NAME = ("16.7M-particle snapshot (2^24, float32): 60% uniform, 25% in 4 Gaussian sheets (sigma 2e-3), "
+                 "15% in 200 Plummer clumps, dN/dM ~ M^-1.6 on [1e-5, 1e-2] M_tot, 10% unbound")
+# bytes per tree point the path must move at least once (pos read, keys, sort, tree, KNN +
+# density, HOP), per unit for the density kernel: read the query (12 B), write the
+# density (8 B), the K_d neighbour list the reference builds (4 * K_d), the radius (4 B)
+DENSITY_BYTES_PER_POINT = 12 + 8 + 4 * KNN + 4
+
+
+def _peaks() -> tuple[float, str]:
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        for k in ("hbm_gbs", "hbm_GBs", "copy_gbs"):
+            if k in d:
+                return float(d[k]), "measured"
+        for v in d.values():
+            if isinstance(v, dict) and "hbm_gbs" in v:
+                return float(v["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.p = None
+        self.out = tempfile.NamedTemporaryFile(prefix="clocks", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.out, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.out.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in Path(self.out.name).read_text().splitlines():
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        os.unlink(self.out.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_records(n: int, seed: int, pinned: bool):
+    """The workload's .lis records in (page-locked) host memory; returns (tensor, spec, 4piG)."""
+    import torch
+
+    import plan_gb300 as pg
+
+    L = pg.lib()
+    spec = pg.SynthSpec()
+    rc = L.plan_synth_default_spec(WORKLOAD, n, seed, C.byref(spec))
+    assert rc == 0
+    spec.nx = NX
+    fourpig = L.plan_synth_four_pi_G_for_mean(C.byref(spec), NX, NX)
+    spec.G = fourpig / (4 * np.pi)
+    rec = torch.empty(n * 44, dtype=torch.uint8, pin_memory=pinned)
+    info = pg.SynthInfo()
+    rc = L.plan_synth_records(C.byref(spec), C.c_void_p(rec.data_ptr()), C.byref(info))
+    assert rc == 0
+    return rec, fourpig
+
+
+def lis_view(pg, ptr: int, n: int):
+    v = pg.LisView()
+    lim = [-0.1, 0.1] * 6
+    for i, x in enumerate(lim):
+        v.coor_lim[i] = float(np.float32(x))
+    v.ntypes = 1
+    v.type_info[0] = 1.0
+    v.time = 0.0
+    v.dt = 0.0
+    v.nblocks = 1
+    arr = (C.c_void_p * 1)(ptr)
+    cnt = (C.c_uint64 * 1)(n)
+    v.records = C.cast(arr, C.POINTER(C.c_void_p))
+    v.counts = C.cast(cnt, C.POINTER(C.c_uint64))
+    v._keep = (arr, cnt)
+    return v
+
+
+def write_params(path: Path, fourpig: float, threads: int) -> None:
+    path.write_text(f"Nx1 = {NX}\nNx2 = {NX}\nNx3 = {NX}\nZ = 0.02\nfour_pi_G_par = {fourpig!r}\nknn = {KNN}\nhop = {HOP}\n"
+                    f"num_threads = {threads}\n")
+
+
+def write_lis(path: Path, rec: np.ndarray, n: int) -> None:
+    import struct
+
+    hdr = struct.pack("<12fi1fffq", *([-0.1, 0.1] * 6), 1, 1.0, 0.0, 0.0, n)
+    with open(path, "wb") as f:
+        f.write(hdr)
+        f.write(memoryview(rec))
+
+
+# ---------------------------------------------------------------- CPU legs
+def cpu_sample(n: int, seed: int, threads: int, reps: int = 1) -> dict:
+    """The oracle restatement on a sample snapshot of the same workload: particles/s."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+
+    with tempfile.TemporaryDirectory() as d:
+        d = Path(d)
+        rec, fourpig = make_records(n, seed, pinned=False)
+        write_lis(d / "Snap.0000.ds.lis", rec.numpy(), n)
+        write_params(d / "para.txt", fourpig, threads)
+        times = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            o = oracle.Oracle(str(d / "Snap.0000.ds.lis"), str(d / "para.txt"), threads=threads, pow_mode=0)
+            o.find()
+            times.append(time.perf_counter() - t0)
+            o.close()
+    return {"n": n, "seconds": times}
+
+
+def run_reference(args) -> None:
+    """The reference arm: the CPU implementation of the path on the host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from plan_gb300 import build as b
+
+    b.build_oracle()
+    threads = os.cpu_count() or 1
+    n = args.sample_n
+    for _ in range(args.warmup):
+        cpu_sample(n, SEED, threads)
+    r = cpu_sample(n, SEED, threads, reps=args.steps)
+    per = [n / t for t in r["seconds"]]
+    value = args.steps * n / sum(r["seconds"])
+    sample = f"{n} particles of the same workload (same mixture and clump mass function, clump count scaled), {args.steps} snapshots"
+    line = {"impl": "reference", "metric": "particles/s", "value": value, "unit": "particles/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(r["seconds"]) / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD_NAME, "n_particles": N_FULL, "sample_particles": n, "knn": KNN, "hop": HOP, "nx": NX},
+            "cpu_baseline": {"value": value, "unit": "particles/s", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "particles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "per_step_particles_per_s": per}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- replicas
+def reduce_max(x: float, dist, device: str = "cpu") -> float:
+    """The slowest replica's time (max over ranks); x unchanged without a process group."""
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_seed(rank: int) -> int:
+    """Each rank finds clumps in its own snapshot (replicas; nothing is exchanged)."""
+    return SEED + rank
+
+
+def aggregate(world: int, n: int, steps: int, total_ms: float) -> float:
+    """Whole-job particles/s: every rank's particles over the slowest rank's time."""
+    return world * n * steps / (total_ms / 1e3)
+
+
+# ---------------------------------------------------------------- GPU arm
+def run_gpu(args) -> None:
+    import torch
+
+    import plan_gb300 as pg
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py: no CUDA device (this path has no CPU fallback)")
+    torch.cuda.set_device(local)
+    n = args.n
+    rec_h, fourpig = make_records(n, replica_seed(rank), pinned=True)
+    rec_d = rec_h.to(f"cuda:{local}")
+    with tempfile.TemporaryDirectory() as d:
+        par = Path(d) / "para.txt"
+        write_params(par, fourpig, os.cpu_count() or 1)
+        p = pg.params(str(par))
+    f = pg.Finder(local)
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+    v_dev = lis_view(pg, rec_d.data_ptr(), n)
+    v_host = lis_view(pg, rec_h.data_ptr(), n)
+    L = pg.lib()
+
+    def step(view):
+        h = C.c_void_p()
+        rc = L.plan_find_clumps(f._h, C.byref(view), C.byref(p), 1, C.c_void_p(sp), C.byref(h))
+        if rc:
+            raise pg.PlanError(rc, f.error())
+        cat = pg.Catalogue(h)
+        nc = len(cat)
+        cat.close()
+        return nc
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    def timed(view, steps):
+        barrier()
+        l0 = f.kernel_launches()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+        per, dens_ms, densest_ms = [], [], []
+        with torch.cuda.stream(stream):
+            ev[0].record(stream)
+            for i in range(steps):
+                step(view)
+                ev[i + 1].record(stream)
+                st = f.stage_times()
+                dens_ms.append(st[20])
+                densest_ms.append(st[21])
+        barrier()
+        per = [ev[i].elapsed_time(ev[i + 1]) for i in range(steps)]
+        total = reduce_max(ev[0].elapsed_time(ev[steps]), dist, f"cuda:{local}")
+        return total, per, f.kernel_launches() - l0, dens_ms, densest_ms
+
+    for _ in range(args.warmup):
+        step(v_dev)
+    clocks = ClockSampler(local)
+    clocks.start()
+    total, per, launches, dens_ms, densest_ms = timed(v_dev, args.steps)
+    clk = clocks.stop()
+    stage = f.stage_times()
+    cnt = f.counters()
+    nclumps = int(cnt[7])
+    tree_points = int(cnt[2])
+    # end to end through the same call with host records
+    step(v_host)
+    total_e2e, per_e2e, _, _, _ = timed(v_host, args.steps)
+    h2d = int(f.counters()[20])
+    d2h = int(f.counters()[21])
+    value = aggregate(world, n, args.steps, total)
+    e2e_value = aggregate(world, n, args.steps, total_e2e)
+    peak, peak_kind = _peaks()
+    dens_avg = float(np.mean(dens_ms))
+    achieved = DENSITY_BYTES_PER_POINT * tree_points / (dens_avg / 1e3) / 1e9
+    roof = {"kernel": "k_density_f (KNN + median density, FP32-filtered exact traversal)", "bound": "hbm", "achieved": achieved,
+            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": f"{peak_kind} HBM copy bandwidth",
+            "traffic": None, "bytes_per_unit": DENSITY_BYTES_PER_POINT, "units_per_launch": tree_points,
+            "launch_ms": dens_avg}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        r = cpu_sample(args.sample_n, SEED, threads)
+        cv = args.sample_n / r["seconds"][0]
+        cpu = {"value": cv, "unit": "particles/s", "cores": threads, "kind": "port",
+               "sample": f"one {args.sample_n}-particle snapshot of the same workload (clump count scaled) through the oracle"}
+    if rank == 0:
+        line = {"metric": "particles/s", "value": value, "unit": "particles/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": total / args.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": WORKLOAD_NAME, "n_particles": n, "seed": SEED, "knn": KNN, "hop": HOP, "nx": NX,
+                           "tree_points": tree_points, "clumps_found": nclumps, "parallelism": f"replicas{world}",
+                           "l2": "inputs larger than L2 (records 738 MB, tree arrays several GB), no flush"},
+                "e2e": {"value": e2e_value, "unit": "particles/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                        "ms_per_step": total_e2e / args.steps},
+                "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
+                "snapshots_per_s": world * args.steps / (total / 1e3),
+                "latency_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99))},
+                "stage_ms": {"ingest_ghosts_keys": stage[0], "sort": stage[1], "sinks_tree": stage[2], "tree_tail": stage[3],
+                             "density": stage[4], "densest": stage[5], "hop": stage[6], "clump_stage": stage[7],
+                             "catalogue": stage[8], "density_kernel": stage[20], "densest_kernel": stage[21]}}
+        print(json.dumps(line), flush=True)
+    f.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
+    ap.add_argument("--n", type=int, default=N_FULL, help="particles per snapshot (default: the full workload)")
+    ap.add_argument("--sample-n", type=int, default=1 << 21, help="particles of the CPU sample snapshot")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -161,6 +161,10 @@ int plan_stage_copy(plan_ctx *ctx, int which, void *host_dst, size_t bytes);
  * k neighbours of each of nq positions (est = 0: the reference's own first radius), sorted
  * ascending as the reference returns them. */
 int plan_knn(plan_ctx *ctx, const double *pos3, uint32_t nq, uint32_t k, double est, uint32_t *idx, double *dr2);
+/* std::sort with AscendingMorton (src/tree.hpp:2269-2273, 2831) of n 96-bit keys given in
+ * input order (3 x u32 each, low word first): order[i] receives the input index of the i-th
+ * sorted key, with equal keys in the order the library's introsort leaves them. */
+int plan_morton_order(plan_ctx *ctx, const uint32_t *keys3, uint32_t n, uint32_t *order);
 /* Wall time per stage of the last snapshot in milliseconds (CUDA events):
  * [0] upload+unpack, [1] ghosts, [2] keys+sort, [3] tree, [4] density KNN, [5] HOP KNN,
  * [6] grouping, [7] clump stage, [8] catalogue download. */

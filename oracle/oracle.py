@@ -44,6 +44,7 @@ def lib() -> C.CDLL:
         L.orc_keys.argtypes = [vp, C.c_void_p]
         L.orc_nodes.argtypes = [vp, C.c_void_p, C.c_void_p]
         L.orc_tree_box.argtypes = [vp, C.c_void_p]
+        L.orc_knn.restype = C.c_int
         L.orc_knn.argtypes = [vp, C.c_void_p, C.c_uint, C.c_double, C.c_void_p, C.c_void_p]
         L.orc_densest.argtypes = [vp, C.c_void_p]
         L.orc_peaks.argtypes = [vp, C.c_void_p]
@@ -52,19 +53,30 @@ def lib() -> C.CDLL:
         L.orc_clumps.restype = u64
         L.orc_clumps.argtypes = [vp, C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_write_outputs.argtypes = [vp, C.c_char_p, C.c_int]
+        L.orc_morton_order.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p]
         _lib = L
     return _lib
+
+
+def morton_order(keys3: np.ndarray) -> np.ndarray:
+    """Input indices in the order std::sort with the reference's Morton comparator leaves them."""
+    k = np.ascontiguousarray(keys3, dtype=np.uint32).reshape(-1, 3)
+    out = np.empty(len(k), dtype=np.uint32)
+    lib().orc_morton_order(k.ctypes.data, len(k), out.ctypes.data)
+    return out
 
 
 class Oracle:
     """One snapshot through the CPU restatement: tree, densities, HOP, clumps."""
 
-    def __init__(self, lis: str, param: str | None, threads: int = 0, pow_mode: int = 0, no_ghost: bool = False):
+    def __init__(self, lis, param: str | None, threads: int = 0, pow_mode: int = 0, no_ghost: bool = False):
+        """lis: one path or the list of files of one snapshot (id0 first)."""
         L = lib()
         self._h = L.orc_open((param or "").encode(), int(threads), int(pow_mode), int(no_ghost))
         if not self._h:
             raise RuntimeError(f"oracle: cannot read parameters {param}")
-        rc = L.orc_load(self._h, str(lis).encode())
+        paths = [lis] if isinstance(lis, (str, bytes)) or not hasattr(lis, "__iter__") else list(lis)
+        rc = L.orc_load(self._h, "\n".join(str(p) for p in paths).encode())
         if rc:
             raise RuntimeError(f"oracle: cannot read {lis} (status {rc})")
 
@@ -110,7 +122,9 @@ class Oracle:
         idx = np.empty((pos.shape[0], k), dtype=np.uint32)
         dr2 = np.empty((pos.shape[0], k))
         for i in range(pos.shape[0]):
-            lib().orc_knn(self._h, pos[i].ctypes.data, k, float(est), idx[i].ctypes.data, dr2[i].ctypes.data)
+            rc = lib().orc_knn(self._h, pos[i].ctypes.data, k, float(est), idx[i].ctypes.data, dr2[i].ctypes.data)
+            if rc:
+                raise LookupError(f"oracle: position {pos[i].tolist()} has no leaf in the tree")
         return idx, dr2
 
     def densest(self) -> np.ndarray:

@@ -510,12 +510,16 @@ inline void heap_add(Heap &h, unsigned k, int i, double dr2) {  // Add2Heaps, sr
 }
 }  // namespace
 
-void Tree::knn(const V3 &pos, unsigned k, Heap &heap, double est) const {  // src/tree.hpp:3198-3251
+bool Tree::knn(const V3 &pos, unsigned k, Heap &heap, double est) const {  // src/tree.hpp:3198-3251
     double r;
     if (est == 0) {
         double r2 = 0;
         if (within(pos, root_center, half_width)) {
             uint32_t node = pos2node(pos);
+            if (node == UINT32_MAX) {
+                heap.clear();
+                return false;
+            }
             while (nodes[node].end - nodes[node].begin < k / 4) node = nodes[node].parent;
             r2 = nodes[node].half_width * nodes[node].half_width;
         } else {
@@ -551,6 +555,7 @@ void Tree::knn(const V3 &pos, unsigned k, Heap &heap, double est) const {  // sr
         r *= 2;
     } while (heap.size() < k);
     std::sort_heap(heap.begin(), heap.end(), LessSecond());
+    return true;
 }
 
 void Tree::ball(const V3 &c, double r, std::vector<uint32_t> &out) const {  // src/tree.hpp:3275-3304

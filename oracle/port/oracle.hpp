@@ -147,7 +147,9 @@ struct Tree {
     bool sphere_contains(const V3 &c, double r, uint32_t node) const;
     bool sphere_intersects(const V3 &c, double r, uint32_t node) const;
     // KNN_Search_OpenMP (src/tree.hpp:3198-3251): heap sorted ascending on return.
-    void knn(const V3 &pos, unsigned k, Heap &heap, double estimated_distance = 0) const;
+    // false when the position has no leaf in the tree (the reference then reports "Key2Leaf:
+    // leaf cell doesn't exist in tree" and continues with an invalid node, src/tree.hpp:2983-2987)
+    bool knn(const V3 &pos, unsigned k, Heap &heap, double estimated_distance = 0) const;
     // BallSearch / RecursiveBallSearchCount (src/tree.hpp:3255-3304).
     void ball(const V3 &c, double r, std::vector<uint32_t> &out) const;
     uint32_t ball_count(const V3 &c, double r) const;

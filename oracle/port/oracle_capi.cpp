@@ -2,6 +2,7 @@
 // Test infrastructure only: the product never links this library.
 #include "oracle.hpp"
 
+#include <algorithm>
 #include <chrono>
 #include <cstring>
 #include <string>
@@ -41,10 +42,19 @@ void *orc_open(const char *param_path, int threads, int pow_mode, int no_ghost) 
 void orc_close(void *h) { delete static_cast<Ctx *>(h); }
 
 // Read one combined .lis file (first file of a run), make ghosts and build the tree.
-int orc_load(void *h, const char *lis_path) {
+// lis_paths: one path, or the files of one snapshot separated by newlines (id0 first)
+int orc_load(void *h, const char *lis_paths) {
     Ctx *c = static_cast<Ctx *>(h);
     double t0 = now();
-    std::vector<std::string> files{lis_path};
+    std::vector<std::string> files;
+    std::string all(lis_paths);
+    for (size_t b = 0; b <= all.size();) {
+        size_t e = all.find('\n', b);
+        if (e == std::string::npos) e = all.size();
+        if (e > b) files.push_back(all.substr(b, e - b));
+        b = e + 1;
+    }
+    if (files.empty()) return 3;
     int rc = read_lis_files(files, c->snap);
     if (rc) return rc;
     finish_read(c->snap, c->par, true);
@@ -123,11 +133,14 @@ void orc_tree_box(void *h, double *out5) {
 }
 
 // KNN of an arbitrary position (est = 0 uses the reference's own first radius).
-void orc_knn(void *h, const double *pos, unsigned k, double est, uint32_t *idx, double *dr2) {
+// Returns 0, or 7 when the position has no leaf in the tree (the reference's Key2Leaf
+// failure; its KNN is undefined there).
+int orc_knn(void *h, const double *pos, unsigned k, double est, uint32_t *idx, double *dr2) {
     auto &t = static_cast<Ctx *>(h)->finder.tree;
     Heap hp;
-    t.knn(V3(pos[0], pos[1], pos[2]), k, hp, est);
+    if (!t.knn(V3(pos[0], pos[1], pos[2]), k, hp, est)) return 7;
     for (unsigned j = 0; j < k; ++j) { idx[j] = (uint32_t)hp[j].first; dr2[j] = hp[j].second; }
+    return 0;
 }
 
 void orc_densest(void *h, uint32_t *out) {
@@ -188,6 +201,18 @@ int orc_write_outputs(void *h, const char *out_path, int first) {
     std::fwrite(s.data(), 1, s.size(), f);
     std::fclose(f);
     return 0;
+}
+
+// The order std::sort with the reference's comparator (low 96 bits only,
+// src/tree.hpp:2269-2273, 2831) gives keys in input order: order[i] = input index of the
+// i-th sorted key.
+void orc_morton_order(const uint32_t *keys3, uint32_t n, uint32_t *order) {
+    typedef unsigned __int128 u128;
+    std::vector<u128> m(n);
+    for (uint32_t i = 0; i < n; ++i)
+        m[i] = ((u128)i << 96) | ((u128)keys3[3 * (size_t)i + 2] << 64) | ((u128)keys3[3 * (size_t)i + 1] << 32) | keys3[3 * (size_t)i];
+    std::sort(m.begin(), m.end(), [](u128 x, u128 y) { return (x << 32) < (y << 32); });
+    for (uint32_t i = 0; i < n; ++i) order[i] = (uint32_t)(m[i] >> 96);
 }
 
 }  // extern "C"

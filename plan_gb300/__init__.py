@@ -111,10 +111,12 @@ def lib() -> C.CDLL:
             "plan_stage_count": (u64, [vp, i32]),
             "plan_stage_copy": (i32, [vp, i32, vp, C.c_size_t]),
             "plan_knn": (i32, [vp, dp, u32, u32, C.c_double, C.POINTER(C.c_uint32), dp]),
+            "plan_morton_order": (i32, [vp, vp, u32, vp]),
             "plan_stage_times": (i32, [vp, dp, i32]),
             "plan_kernel_launches": (u64, [vp]),
             "plan_counters": (i32, [vp, C.POINTER(C.c_uint64), i32]),
             "plan_synth_default_spec": (i32, [i32, u64, u64, C.POINTER(SynthSpec)]),
+            "plan_synth_records": (i32, [C.POINTER(SynthSpec), vp, C.POINTER(SynthInfo)]),
             "plan_synth_write_lis": (i32, [C.c_char_p, C.POINTER(SynthSpec), C.POINTER(SynthInfo)]),
             "plan_synth_four_pi_G_for_mean": (C.c_double, [C.POINTER(SynthSpec), C.c_int32, C.c_int32]),
         }
@@ -131,7 +133,7 @@ EXPORTED = [
     "plan_lis_time", "plan_lis_get_view", "plan_ctx_create", "plan_ctx_destroy", "plan_last_error", "plan_footprint_bytes",
     "plan_build_tree", "plan_find_planetesimals", "plan_find_clumps", "plan_catalogue_free", "plan_catalogue_count",
     "plan_catalogue_get", "plan_catalogue_summary", "plan_catalogue_write_peaks", "plan_catalogue_basic_results",
-    "plan_stage_count", "plan_stage_copy", "plan_knn", "plan_stage_times", "plan_kernel_launches", "plan_counters",
+    "plan_stage_count", "plan_stage_copy", "plan_knn", "plan_morton_order", "plan_stage_times", "plan_kernel_launches", "plan_counters",
     "plan_synth_default_spec", "plan_synth_records", "plan_synth_write_lis", "plan_synth_four_pi_G_for_mean",
 ]
 
@@ -309,6 +311,15 @@ class Finder:
         if rc:
             raise PlanError(rc, self.error())
         return idx, dr2
+
+    def morton_order(self, keys3: np.ndarray) -> np.ndarray:
+        """Input indices in std::sort order of 96-bit keys (reference comparator)."""
+        k = np.ascontiguousarray(keys3, dtype=np.uint32).reshape(-1, 3)
+        out = np.empty(len(k), dtype=np.uint32)
+        rc = lib().plan_morton_order(self._h, k.ctypes.data, len(k), out.ctypes.data)
+        if rc:
+            raise PlanError(rc, self.error())
+        return out
 
     def stage_times(self) -> np.ndarray:
         a = np.zeros(32)

@@ -8,6 +8,7 @@
 #include "catalogue.h"
 #include "hop.h"
 #include "pipeline.h"
+#include "sort.h"
 
 namespace plan {
 
@@ -77,7 +78,8 @@ int plan_ctx_create(int device, plan_ctx **out) {
     g_ctx = &c;
     c.device = device;
     if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaMalloc(&c.d_err, 16) != cudaSuccess || cudaMemset(c.d_err, 0, 16) != cudaSuccess) {
+        cudaMalloc(&c.d_err, 16) != cudaSuccess || cudaMemset(c.d_err, 0, 16) != cudaSuccess ||
+        cudaEventCreate(&c.kev[0]) != cudaSuccess || cudaEventCreate(&c.kev[1]) != cudaSuccess) {
         delete h;
         return kErrDevice;
     }
@@ -93,6 +95,8 @@ void plan_ctx_destroy(plan_ctx *h) {
     if (c.arena.base) cudaFree(c.arena.base);
     if (c.scratch.base) cudaFree(c.scratch.base);
     if (c.d_err) cudaFree(c.d_err);
+    for (auto &e : c.kev)
+        if (e) cudaEventDestroy(e);
     if (c.stream) cudaStreamDestroy(c.stream);
     if (g_ctx == &c) g_ctx = nullptr;
     delete h;
@@ -140,6 +144,8 @@ int plan_find_planetesimals(plan_ctx *h, plan_params *p, void *stream, plan_cata
     cudaSetDevice(c.device);
     if (!c.tree.Tu) return kErrArgument;
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c.stream;
+    if (out) *out = nullptr;
+    cudaMemsetAsync(c.d_err, 0, 16, s);
     int rc = find_planetesimals(c, *p, s, out);
     unsigned err = 0;
     cudaMemcpy(&err, c.d_err, 4, cudaMemcpyDeviceToHost);
@@ -147,6 +153,10 @@ int plan_find_planetesimals(plan_ctx *h, plan_params *p, void *stream, plan_cata
     if (rc == kOk && err) {
         c.last_error = "device error flags " + std::to_string(err) + " while finding clumps";
         rc = kErrDeviceLimit;
+        if (out && *out) {
+            plan_catalogue_free(*out);
+            *out = nullptr;
+        }
     }
     return c.status_from(rc, "plan_find_planetesimals");
 }
@@ -233,7 +243,51 @@ int plan_knn(plan_ctx *h, const double *pos3, uint32_t nq, uint32_t k, double es
     Context &c = h->c;
     g_ctx = &c;
     cudaSetDevice(c.device);
-    return c.status_from(knn_positions(c, pos3, nq, k, est, idx, dr2), "plan_knn");
+    c.last_error.clear();
+    cudaMemsetAsync(c.d_err, 0, 16, c.stream);
+    int rc = knn_positions(c, pos3, nq, k, est, idx, dr2);
+    unsigned err = 0;
+    cudaMemcpy(&err, c.d_err, 4, cudaMemcpyDeviceToHost);
+    if (rc == kOk && (err & kDevErrKey2Leaf)) {
+        c.last_error = "a query position has no leaf in the tree (the reference's Key2Leaf failure; its KNN is undefined there)";
+        rc = kErrUnsupported;
+    } else if (rc == kOk && err) {
+        c.last_error = "device error flags " + std::to_string(err) + " in the KNN";
+        rc = kErrDeviceLimit;
+    }
+    return c.status_from(rc, "plan_knn");
+}
+
+int plan_morton_order(plan_ctx *h, const uint32_t *keys3, uint32_t n, uint32_t *order) {
+    if (!h || (n && (!keys3 || !order))) return kErrArgument;
+    Context &c = h->c;
+    g_ctx = &c;
+    c.last_error.clear();
+    cudaSetDevice(c.device);
+    if (n == 0) return kOk;
+    cudaStream_t s = c.stream;
+    std::vector<uint32_t> w(4 * (size_t)n);
+    for (uint32_t i = 0; i < n; ++i) {
+        w[i] = keys3[3 * (size_t)i];
+        w[(size_t)n + i] = keys3[3 * (size_t)i + 1];
+        w[2 * (size_t)n + i] = keys3[3 * (size_t)i + 2];
+        w[3 * (size_t)n + i] = i;
+    }
+    uint32_t *d = nullptr;
+    void *scr = nullptr;
+    const size_t sb = morton_sort_scratch_bytes(n);
+    int rc = kOk;
+    if (cudaMallocAsync(&d, w.size() * 4, s) != cudaSuccess || cudaMallocAsync(&scr, sb, s) != cudaSuccess) {
+        cudaGetLastError();
+        rc = kErrOutOfMemory;
+    }
+    if (!rc && cudaMemcpyAsync(d, w.data(), w.size() * 4, cudaMemcpyHostToDevice, s) != cudaSuccess) rc = kErrDevice;
+    if (!rc) rc = morton_sort_std(c, d, d + n, d + 2 * (size_t)n, d + 3 * (size_t)n, n, scr, sb, s);
+    if (!rc && cudaMemcpyAsync(order, d + 3 * (size_t)n, (size_t)n * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) rc = kErrDevice;
+    if (d) cudaFreeAsync(d, s);
+    if (scr) cudaFreeAsync(scr, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess && !rc) rc = kErrDevice;
+    return c.status_from(rc, "plan_morton_order");
 }
 
 int plan_stage_times(const plan_ctx *h, double *ms, int n) {

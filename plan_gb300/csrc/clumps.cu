@@ -8,7 +8,8 @@
 // growing a clump writes a new segment.
 //
 // Sequential semantics are kept where the reference has them:
-//  * sums run in member order on one thread (kinematics, dispersion, two-sigma mass, J);
+//  * sums run in member order (kinematics, dispersion, two-sigma mass, J): the terms of
+//    32 members are formed by a warp, then one lane per sum adds them in order;
 //  * merge sweeps evaluate every candidate pair in parallel (ball search over a clump tree,
 //    boundness, saddle densities by KNN), then one thread resolves predator/prey in key
 //    order; predators merge in waves so a predator that is itself eaten later is complete
@@ -16,8 +17,9 @@
 //  * unbinding scans members from the outermost inwards with the current state; a chunk of
 //    candidates is evaluated in parallel and the highest-index unbound member is removed
 //    before the rest is re-evaluated (exact, since only removals change the state);
-//  * Hill-sphere rebinding runs clump by clump in key order (the in-clump flags couple
-//    clumps); inside a clump the first bound candidate of each chunk is accepted the same way.
+//  * Hill-sphere rebinding runs all clumps at once under an ordered-claim rule and reruns
+//    those that conflicted, which gives the clump-by-clump result in key order; inside a
+//    clump the first bound candidate of each chunk is accepted the same way as unbinding.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -107,25 +109,48 @@ __global__ void k_init(uint32_t C, const uint32_t *gkey, const uint32_t *goff, C
     slot_of_key[k] = g;
 }
 
-// CalculateKinematicProperties (src/tree.hpp:4431-4442): one thread per clump, in order.
-__global__ void k_kinematics(const uint32_t *list, uint32_t n, CT ct, Pool P, const double4_32a *pos, const double4_32a *vel, int with_hill,
-                             double G, double Omega) {
-    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+// CalculateKinematicProperties (src/tree.hpp:4431-4442), one warp per clump. The products
+// m*x, m*v of a tile of 32 members are formed by all lanes at once; lanes 0..6 then each run
+// one of the seven running sums strictly in member order, so every sum rounds exactly as
+// the reference's loop (on this GPU each dependent FP64 add costs ~63 cycles, which makes
+// the add chains, not the products, the limit).
+__global__ void __launch_bounds__(128) k_kinematics(const uint32_t *list, uint32_t n, CT ct, Pool P, const double4_32a *pos,
+                                                    const double4_32a *vel, int with_hill, double G, double Omega) {
+    __shared__ double tile[4][7][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t t = blockIdx.x * 4 + wid;
     if (t >= n) return;
-    uint32_t s = list[t];
-    double M = 0, cx = 0, cy = 0, cz = 0, vx = 0, vy = 0, vz = 0;
+    const uint32_t s = list[t];
     const uint32_t o = ct.moff[s], m = ct.mn[s];
-    for (uint32_t k = 0; k < m; ++k) {
-        uint32_t i = P.idx[o + k];
-        double4_32a p = pos[i], v = vel[i];
-        M = M + p.w;
-        cx = cx + p.x * p.w; cy = cy + p.y * p.w; cz = cz + p.z * p.w;
-        vx = vx + v.x * p.w; vy = vy + v.y * p.w; vz = vz + v.z * p.w;
+    double acc = 0;  // lane c < 7 holds sum c: M, m*x, m*y, m*z, m*vx, m*vy, m*vz
+    for (uint32_t base = 0; base < m; base += 32) {
+        const uint32_t k = base + lane;
+        if (k < m) {
+            uint32_t i = P.idx[o + k];
+            double4_32a p = pos[i], v = vel[i];
+            tile[wid][0][lane] = p.w;
+            tile[wid][1][lane] = p.x * p.w;
+            tile[wid][2][lane] = p.y * p.w;
+            tile[wid][3][lane] = p.z * p.w;
+            tile[wid][4][lane] = v.x * p.w;
+            tile[wid][5][lane] = v.y * p.w;
+            tile[wid][6][lane] = v.z * p.w;
+        }
+        __syncwarp();
+        const uint32_t cnt = min(32u, m - base);
+        if (lane < 7)
+            for (uint32_t j = 0; j < cnt; ++j) acc = acc + tile[wid][lane][j];
+        __syncwarp();
     }
-    ct.M[s] = M;
-    ct.com[s] = make_double4_32a(cx / M, cy / M, cz / M, 0);
-    ct.vcom[s] = make_double4_32a(vx / M, vy / M, vz / M, 0);
-    if (with_hill) ct.hill[s] = cr_pow_third(M * G / 3. / Omega / Omega);  // src/tree.hpp:4715-4717
+    double M = __shfl_sync(0xffffffffu, acc, 0);
+    double cx = __shfl_sync(0xffffffffu, acc, 1), cy = __shfl_sync(0xffffffffu, acc, 2), cz = __shfl_sync(0xffffffffu, acc, 3);
+    double vx = __shfl_sync(0xffffffffu, acc, 4), vy = __shfl_sync(0xffffffffu, acc, 5), vz = __shfl_sync(0xffffffffu, acc, 6);
+    if (lane == 0) {
+        ct.M[s] = M;
+        ct.com[s] = make_double4_32a(cx / M, cy / M, cz / M, 0);
+        ct.vcom[s] = make_double4_32a(vx / M, vy / M, vz / M, 0);
+        if (with_hill) ct.hill[s] = cr_pow_third(M * G / 3. / Omega / Omega);  // src/tree.hpp:4715-4717
+    }
 }
 
 // distances to the centre of mass (src/tree.hpp:4448-4450, 4545-4547)
@@ -218,17 +243,36 @@ __global__ void k_one10th(const uint32_t *list, CT ct, Pool P, const double4_32a
     ct.r2s[s] = r2s;
 }
 
-// IsPositionDispersion2Large (src/tree.hpp:4516-4528): sequential sum of squares
-__global__ void k_dispersion(const uint32_t *list, uint32_t n, CT ct, Pool P, double tol, uint8_t *too_large) {
-    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+// IsPositionDispersion2Large (src/tree.hpp:4516-4528): squares formed by the warp, their sum
+// taken in order by lane 0
+__global__ void __launch_bounds__(128) k_dispersion(const uint32_t *list, uint32_t n, CT ct, Pool P, double tol, uint8_t *too_large) {
+    __shared__ double tile[4][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t t = blockIdx.x * 4 + wid;
     if (t >= n) return;
-    uint32_t s = list[t];
+    const uint32_t s = list[t];
     const uint32_t o = ct.moff[s], m = ct.mn[s];
-    if (m == 0) { too_large[t] = 0; return; }
+    if (m == 0) {
+        if (lane == 0) too_large[t] = 0;
+        return;
+    }
     double acc = 0.0;
-    for (uint32_t k = 0; k < m; ++k) acc = acc + P.dist[o + k] * P.dist[o + k];
-    double x = tol * P.dist[o + m - 1];
-    too_large[t] = (acc / (double)m > x * x) ? 1 : 0;
+    for (uint32_t base = 0; base < m; base += 32) {
+        const uint32_t k = base + lane;
+        if (k < m) {
+            double d = P.dist[o + k];
+            tile[wid][lane] = d * d;
+        }
+        __syncwarp();
+        const uint32_t cnt = min(32u, m - base);
+        if (lane == 0)
+            for (uint32_t j = 0; j < cnt; ++j) acc = acc + tile[wid][j];
+        __syncwarp();
+    }
+    if (lane == 0) {
+        double x = tol * P.dist[o + m - 1];
+        too_large[t] = (acc / (double)m > x * x) ? 1 : 0;
+    }
 }
 
 __global__ void k_hill(const uint32_t *list, uint32_t n, CT ct, double G, double Omega) {
@@ -601,77 +645,145 @@ __global__ void __launch_bounds__(256) k_unbind(const uint32_t *list, CT ct, Poo
     }
 }
 
-// Hill-sphere rebinding (src/tree.hpp:4678-4711). A resumable depth-first walk yields the
-// ball's points in the order of RecursiveBallSearch; one block per clump evaluates them a
-// chunk at a time against the clump's current state and takes the first bound one.
-struct BallWalk {
-    uint32_t node, pos, end;
-    uint8_t partial, done;
-};
+// Hill-sphere rebinding (src/tree.hpp:4678-4711).
+//
+// RecursiveBallSearch visits the children of a node in order and every node covers a
+// contiguous run of the Morton-sorted points, so the ball's points come out in ascending
+// point index. The candidates of one SearchBoundParticlesWithinHillRadius call are therefore
+// the ball's points that pass the call-independent tests (not marked in a clump before
+// rebinding, density not below the threshold), in ascending index. Those points form the
+// sorted list E (with epos[p] = entries of E below p), so a node's candidates are the slice
+// E[epos[beg], epos[end]) and nodes with an empty slice are skipped without a test.
+//
+// One block per clump: a breadth-first frontier of at most kFront nodes is built in shared
+// memory (stable, so it stays in point order); each thread then walks the subtrees of its
+// frontier entries, once to count and once to write the candidates at scanned offsets.
+constexpr int kFront = 2048;
+constexpr int kRebindThreads = 256;
 
-__device__ bool ball_walk_advance(const KTree &t, double cx, double cy, double cz, double r, BallWalk &w, unsigned *err) {
+__global__ void k_elig_flags(uint32_t Tu, const uint8_t *in_clump, const double *dens, double thr, uint32_t *flag) {
+    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < Tu) flag[q] = (in_clump[q] == 0 && !(dens[q] < thr)) ? 1u : 0u;
+}
+
+__global__ void k_elig_compact(uint32_t Tu, const uint8_t *in_clump, const double *dens, double thr, const uint32_t *epos, uint32_t *E) {
+    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < Tu && in_clump[q] == 0 && !(dens[q] < thr)) E[epos[q]] = q;
+}
+
+// exclusive scan of a[0, n) in shared memory by the whole block (n <= kFront); returns the total
+__device__ uint32_t block_scan_excl(uint32_t *a, uint32_t n, uint32_t *warp_tot) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
+    const uint32_t b = threadIdx.x * per, e = min(n, b + per);
+    uint32_t sum = 0;
+    for (uint32_t i = b; i < e; ++i) sum += a[i];
+    uint32_t incl = sum;
+    for (int d = 1; d < 32; d <<= 1) {
+        uint32_t v = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += v;
+    }
+    if (lane == 31) warp_tot[wid] = incl;
+    __syncthreads();
+    uint32_t before = 0, total = 0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+        if (k < wid) before += warp_tot[k];
+        total += warp_tot[k];
+    }
+    uint32_t run = before + incl - sum;
+    for (uint32_t i = b; i < e; ++i) {
+        uint32_t v = a[i];
+        a[i] = run;
+        run += v;
+    }
+    __syncthreads();
+    return total;
+}
+
+// Node classes of the frontier: 1 contained (all candidates), 2 leaf reached but not
+// contained (candidates filtered by distance), 3 nothing, 4 descend into the children.
+__device__ __forceinline__ int ball_class(const KTree &t, const uint32_t *epos, uint32_t node, double cx, double cy, double cz, double r,
+                                          uint32_t &eb, uint32_t &ee) {
+    eb = epos[t.nbeg[node]];
+    ee = epos[t.nend[node]];
+    if (eb == ee) return 3;
+    const double4_32a nc = t.ncf[node];
+    if (node_contained(nc, cx, cy, cz, r)) return 1;
+    if (node_intersects(nc, cx, cy, cz, r)) return t.nnd[node] == 0 ? 2 : 4;
+    return 3;
+}
+
+// the candidates below a class-4 node f, in point order
+template <class Emit>
+__device__ void ball_walk_below(const KTree &t, const uint32_t *epos, uint32_t f, double cx, double cy, double cz, double r, Emit emit,
+                                unsigned *err) {
+    uint32_t node = t.nfd[f];
     for (uint32_t guard = 0; guard < 4u * t.nodes + 8u; ++guard) {
-        if (w.done) return false;
-        const uint32_t node = w.node;
         if (node >= t.nodes) {
             atomicOr(err, (unsigned)kDevErrBadNode);
-            w.done = 1;
-            return false;
+            return;
         }
-        double4_32a nc = t.ncf[node];
-        int visit = 0;
-        bool down = false;
-        if (node_contained(nc, cx, cy, cz, r)) visit = 1;
-        else if (node_intersects(nc, cx, cy, cz, r)) {
-            if (t.nnd[node] == 0) visit = 2;
-            else down = true;
+        uint32_t eb, ee;
+        const int cls = ball_class(t, epos, node, cx, cy, cz, r, eb, ee);
+        if (cls == 1 || cls == 2) emit(eb, ee, cls == 2);
+        if (cls == 4) {
+            node = t.nfd[node];
+            continue;
         }
-        if (down) {
-            w.node = t.nfd[node];
-        } else {
-            uint32_t n2 = node;
-            while (n2 != 0) {
-                uint32_t p = t.npar[n2];
-                if (n2 + 1 < t.nfd[p] + t.nnd[p]) { n2 = n2 + 1; break; }
-                n2 = p;
+        for (;;) {  // next sibling, climbing back towards f
+            const uint32_t p = t.npar[node];
+            if (node + 1 < t.nfd[p] + t.nnd[p]) {
+                ++node;
+                break;
             }
-            if (n2 == 0) w.done = 1;
-            w.node = n2;
-        }
-        if (visit) {
-            w.pos = t.nbeg[node];
-            w.end = t.nend[node];
-            w.partial = visit == 2;
-            return true;
+            node = p;
+            if (node == f) return;
         }
     }
     atomicOr(err, (unsigned)kDevErrLoopLimit);
-    w.done = 1;
-    return false;
+}
+
+// Deferral records of a clump: the key ranks of the earlier clumps whose particles it
+// skipped (at most kDeferSlots distinct ranks; beyond that only the largest is known and
+// the host falls back to it).
+constexpr int kDeferSlots = 8;
+
+__device__ void defer_add(uint32_t *dset, uint8_t *dover, uint32_t *dmax, uint32_t slot, uint32_t ow) {
+    atomicMax(&dmax[slot], ow + 1);
+    uint32_t *d = dset + (size_t)slot * kDeferSlots;
+    for (int j = 0; j < kDeferSlots; ++j) {
+        const uint32_t v = d[j];  // a set entry never changes again
+        if (v == ow) return;
+        if (v == kNone) {
+            const uint32_t old = atomicCAS(&d[j], kNone, ow);
+            if (old == kNone || old == ow) return;
+        }
+    }
+    dover[slot] = 1;
 }
 
 // One SearchBoundParticlesWithinHillRadius call for every listed clump (one block each).
 // seq_mode = 1: the reference's shared in-clump flags, one clump at a time.
 // seq_mode = 0: clumps run concurrently. owner[q] holds the key rank of the clump holding
 // particle q. A clump treats q as taken if it was marked before rebinding, or is held by
-// itself or by an earlier clump (recording that it deferred, in dmax); it may take q from a
+// itself or by an earlier clump (recording that it deferred, with defer_add); it may take q from a
 // later clump, which is then invalid. A clump that loses q to an earlier one is invalid.
 // Invalid clumps are restored and rerun by the host until none is left; the clumps below
 // the lowest invalid rank are final after every pass, so this ends.
-__global__ void __launch_bounds__(256) k_rebind_round(const uint32_t *list, CT ct, Pool P, KTree t, const double4_32a *vel,
-                                                      const double *dens, uint8_t *in_clump, uint32_t *owner, const uint32_t *rank_of,
-                                                      const uint32_t *slot_of_rank, uint8_t *invalid, uint32_t *dmax, int seq_mode, CP cp,
-                                                      uint8_t *grew, uint32_t *mn_out, unsigned *err) {
+__global__ void __launch_bounds__(kRebindThreads) k_rebind_round(const uint32_t *list, CT ct, Pool P, KTree t, const double4_32a *vel,
+                                                                 const uint32_t *E, const uint32_t *epos, uint8_t *in_clump, uint32_t *owner,
+                                                                 const uint32_t *rank_of, const uint32_t *slot_of_rank, uint8_t *invalid,
+                                                                 uint32_t *dmax, uint32_t *dset, uint8_t *dover, int seq_mode, CP cp,
+                                                                 uint8_t *grew, uint32_t *mn_out,
+                                                                 unsigned *err) {
     __shared__ double sM, scx, scy, scz, svx, svy, svz, c0x, c0y, c0z, rad;
-    __shared__ uint32_t s_nel, s_first, s_noff, s_len, s_nacc;
-    __shared__ BallWalk w;
-    __shared__ uint32_t chunk[256];
-    __shared__ uint8_t cpart[256];
-    __shared__ uint32_t warp_cnt[8];
+    __shared__ uint32_t s_first, s_noff, s_nacc, s_nf, s_expand;
+    __shared__ uint32_t front[kFront], front2[kFront], fcnt[kFront];
+    __shared__ uint8_t fcls[kFront], fcls2[kFront];
+    __shared__ uint32_t warp_tot[kRebindThreads / 32];
     const uint32_t slot = list[blockIdx.x];
     const uint32_t myrank = seq_mode ? 0u : rank_of[slot];
     const double4_32a *pos = t.pos;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     if (threadIdx.x == 0) {
         sM = ct.M[slot];
         double4_32a c = ct.com[slot], v = ct.vcom[slot];
@@ -679,81 +791,114 @@ __global__ void __launch_bounds__(256) k_rebind_round(const uint32_t *list, CT c
         svx = v.x; svy = v.y; svz = v.z;
         c0x = c.x; c0y = c.y; c0z = c.z;  // the ball stays where the call started
         rad = ct.hill[slot];
-        w = BallWalk{0, 0, 0, 0, 0};
-        s_nel = 0;
         s_nacc = 0;
+        front[0] = 0;
+        fcls[0] = 0;
+        s_nf = 1;
     }
     __syncthreads();
-    const double rr = rad * rad;
-    // 0) count the eligible candidates (state-independent tests) to size the segment
-    for (int pass = 0; pass < 2; ++pass) {
-        for (;;) {
-            if (threadIdx.x == 0) {
-                uint32_t len = 0;
-                while (len < blockDim.x) {
-                    if (w.pos < w.end) {
-                        chunk[len] = w.pos;
-                        cpart[len] = w.partial;
-                        ++w.pos;
-                        ++len;
-                    } else if (!ball_walk_advance(t, c0x, c0y, c0z, rad, w, err)) {
-                        break;
-                    }
+    const double cx = c0x, cy = c0y, cz = c0z, r = rad, rr = r * r;
+    // 1) breadth-first frontier (classes 1..4; 0 = not yet classified)
+    for (int level = 0; level < 40; ++level) {
+        const uint32_t nf = s_nf;
+        if (threadIdx.x == 0) s_expand = 0;
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < nf; i += blockDim.x) {
+            uint32_t node = front[i];
+            int cls = fcls[i];
+            if (cls == 0) {
+                if (node >= t.nodes) {
+                    atomicOr(err, (unsigned)kDevErrBadNode);
+                    cls = 3;
+                } else {
+                    uint32_t eb, ee;
+                    cls = ball_class(t, epos, node, cx, cy, cz, r, eb, ee);
                 }
-                s_len = len;
+                fcls[i] = (uint8_t)cls;
             }
-            __syncthreads();
-            const uint32_t len = s_len;
-            if (len == 0) break;
-            bool keep = false;
-            uint32_t q = 0;
-            if (threadIdx.x < len) {
-                q = chunk[threadIdx.x];
-                const double4_32a p = pos[q];
-                // RecursiveBallSearch keeps leaf points within r; contained nodes pass whole
-                bool inside = !cpart[threadIdx.x] || point_dr2(c0x, c0y, c0z, p) <= rr;
-                keep = inside && in_clump[q] == 0 && !(dens[q] < cp.thr);
-                if (keep && !seq_mode) {
-                    uint32_t ow = owner[q];
-                    if (ow != kNone && ow <= myrank) {  // held by this or an earlier clump
-                        keep = false;
-                        if (ow < myrank && pass == 1) atomicMax(&dmax[slot], ow + 1);
-                    }
+            fcnt[i] = cls == 4 ? t.nnd[node] : (cls == 3 ? 0u : 1u);
+            if (cls == 4) s_expand = 1;
+        }
+        __syncthreads();
+        if (!s_expand) break;
+        const uint32_t total = block_scan_excl(fcnt, nf, warp_tot);
+        if (total > (uint32_t)kFront) break;
+        for (uint32_t i = threadIdx.x; i < nf; i += blockDim.x) {
+            const int cls = fcls[i];
+            const uint32_t o = fcnt[i];
+            if (cls == 1 || cls == 2) {
+                front2[o] = front[i];
+                fcls2[o] = (uint8_t)cls;
+            } else if (cls == 4) {
+                const uint32_t c0 = t.nfd[front[i]], nc = t.nnd[front[i]];
+                for (uint32_t c = 0; c < nc; ++c) {
+                    front2[o + c] = c0 + c;
+                    fcls2[o + c] = 0;
                 }
             }
-            unsigned bal = __ballot_sync(0xffffffffu, keep);
-            if (lane == 0) warp_cnt[wid] = __popc(bal);
-            __syncthreads();
-            if (pass == 1) {
-                uint32_t before = 0;
-                for (int k = 0; k < wid; ++k) before += warp_cnt[k];
-                if (keep) P.idx[s_noff + ct.mn[slot] + s_nel + before + __popc(bal & ((1u << lane) - 1u))] = q;
-            }
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                uint32_t tot = 0;
-                for (int k = 0; k < (int)(blockDim.x / 32); ++k) tot += warp_cnt[k];
-                s_nel += tot;
-            }
-            __syncthreads();
         }
-        if (pass == 0) {
-            // segment: the members, the eligible candidates in walk order, then the accepted
-            // ones (at most one per eligible candidate)
-            if (threadIdx.x == 0) {
-                s_noff = pool_alloc(P, ct.mn[slot] + 2 * s_nel, err);
-                w = BallWalk{0, 0, 0, 0, 0};
-                s_nel = 0;
-            }
-            __syncthreads();
-            if (s_noff == kNone) return;
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < total; i += blockDim.x) {
+            front[i] = front2[i];
+            fcls[i] = fcls2[i];
         }
+        if (threadIdx.x == 0) s_nf = total;
+        __syncthreads();
     }
+    const uint32_t nf = s_nf;
+    for (uint32_t i = threadIdx.x; i < nf; i += blockDim.x) {  // entries left unclassified by the level cap
+        if (fcls[i] != 0) continue;
+        uint32_t eb, ee;
+        fcls[i] = front[i] < t.nodes ? (uint8_t)ball_class(t, epos, front[i], cx, cy, cz, r, eb, ee) : (uint8_t)3;
+    }
+    __syncthreads();
+    // 2) count the candidates below each frontier entry, then scan to offsets
+    for (uint32_t i = threadIdx.x; i < nf; i += blockDim.x) {
+        const uint32_t node = front[i];
+        const int cls = fcls[i];
+        uint32_t cnt = 0;
+        auto count = [&](uint32_t eb, uint32_t ee, bool partial) {
+            if (!partial) {
+                cnt += ee - eb;
+            } else {
+                for (uint32_t j = eb; j < ee; ++j) cnt += point_dr2(cx, cy, cz, pos[E[j]]) <= rr ? 1u : 0u;
+            }
+        };
+        if (cls == 1 || cls == 2) {
+            count(epos[t.nbeg[node]], epos[t.nend[node]], cls == 2);
+        } else if (cls == 4) {
+            ball_walk_below(t, epos, node, cx, cy, cz, r, count, err);
+        }
+        fcnt[i] = cnt;
+    }
+    __syncthreads();
+    const uint32_t nel = block_scan_excl(fcnt, nf, warp_tot);
+    // segment: the members, the candidates in walk order, then the accepted ones (at most
+    // one per candidate)
+    if (threadIdx.x == 0) s_noff = pool_alloc(P, ct.mn[slot] + 2 * nel, err);
+    __syncthreads();
+    if (s_noff == kNone) return;
     const uint32_t m0 = ct.mn[slot], o = ct.moff[slot], no = s_noff;
     for (uint32_t k = threadIdx.x; k < m0; k += blockDim.x) P.idx[no + k] = P.idx[o + k];
-    uint32_t *elig = P.idx + no + m0;  // eligible candidates in walk order
-    // 2) the reference's sequential acceptance over the eligible candidates, a chunk at a time
-    const uint32_t nel = s_nel;
+    uint32_t *elig = P.idx + no + m0;  // candidates in walk order
+    for (uint32_t i = threadIdx.x; i < nf; i += blockDim.x) {
+        const uint32_t node = front[i];
+        const int cls = fcls[i];
+        uint32_t w = fcnt[i];
+        auto fill = [&](uint32_t eb, uint32_t ee, bool partial) {
+            for (uint32_t j = eb; j < ee; ++j) {
+                const uint32_t q = E[j];
+                if (!partial || point_dr2(cx, cy, cz, pos[q]) <= rr) elig[w++] = q;
+            }
+        };
+        if (cls == 1 || cls == 2) {
+            fill(epos[t.nbeg[node]], epos[t.nend[node]], cls == 2);
+        } else if (cls == 4) {
+            ball_walk_below(t, epos, node, cx, cy, cz, r, fill, err);
+        }
+    }
+    __syncthreads();
+    // 3) the reference's sequential acceptance over the candidates, a chunk at a time
     uint32_t *acc = elig + nel;  // accepted, in acceptance order
     uint32_t at = 0;
     while (at < nel) {
@@ -767,7 +912,7 @@ __global__ void __launch_bounds__(256) k_rebind_round(const uint32_t *list, CT c
             if (!taken && !seq_mode) {
                 uint32_t ow = owner[q2];
                 taken = ow != kNone && ow <= myrank;
-                if (ow != kNone && ow < myrank) atomicMax(&dmax[slot], ow + 1);
+                if (ow != kNone && ow < myrank) defer_add(dset, dover, dmax, slot, ow);
             }
             if (!taken) {
                 const double4_32a p = pos[q2], v = vel[q2];
@@ -828,7 +973,7 @@ __global__ void __launch_bounds__(256) k_rebind_round(const uint32_t *list, CT c
 __global__ void k_rebind_restore(const uint32_t *list, uint32_t n, CT ct, Pool P, const double *bM, const double *bh, const double *bri,
                                  const double *bro, const double *br10, const double *br2, const double4_32a *bc, const double4_32a *bv,
                                  const uint32_t *bo, const uint32_t *bn, const uint32_t *bidx, const double *bdist, uint8_t *invalid,
-                                 uint32_t *dmax, unsigned *err) {
+                                 uint32_t *dmax, uint32_t *dset, uint8_t *dover, unsigned *err) {
     __shared__ uint32_t s_off;
     uint32_t t = blockIdx.x;
     if (t >= n) return;
@@ -839,6 +984,8 @@ __global__ void k_rebind_restore(const uint32_t *list, uint32_t n, CT ct, Pool P
         s_off = pool_alloc(P, bn[sl], err);
         invalid[sl] = 0;
         dmax[sl] = 0;
+        dover[sl] = 0;
+        for (int j = 0; j < kDeferSlots; ++j) dset[(size_t)sl * kDeferSlots + j] = kNone;
     }
     __syncthreads();
     if (s_off == kNone) return;
@@ -900,27 +1047,44 @@ __global__ void k_rip(uint32_t C, CT ct, Pool P, uint8_t *pending, uint32_t *cha
     changed[atomicAdd(nchanged, 1u)] = s;
 }
 
-// CalculateAngularMomentum sums (src/tree.hpp:4721-4747), unnormalised
-__global__ void k_angmom(const uint32_t *list, uint32_t n, CT ct, Pool P, const double4_32a *pos, const double4_32a *vel, CP cp) {
-    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+// CalculateAngularMomentum sums (src/tree.hpp:4721-4747), unnormalised: per-member terms by
+// the warp, the three running sums in member order by lanes 0..2
+__global__ void __launch_bounds__(128) k_angmom(const uint32_t *list, uint32_t n, CT ct, Pool P, const double4_32a *pos,
+                                                const double4_32a *vel, CP cp) {
+    __shared__ double tile[4][3][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t t = blockIdx.x * 4 + wid;
     if (t >= n) return;
-    uint32_t s = list[t];
+    const uint32_t s = list[t];
     const uint32_t o = ct.moff[s], m = ct.mn[s];
-    double4_32a c = ct.com[s], vc = ct.vcom[s];
-    double jx = 0, jy = 0, jz = 0;
-    for (uint32_t k = 0; k < m; ++k) {
-        uint32_t i = P.idx[o + k];
-        double4_32a p = pos[i], v = vel[i];
-        double drx = p.x - c.x, dry = p.y - c.y, drz = p.z - c.z;
-        double sx = 0. * p.x, sy = cp.shear * p.x, sz = 0. * p.x;
-        double cx0 = 0. * c.x, cy0 = cp.shear * c.x, cz0 = 0. * c.x;
-        double dvx = (v.x - sx) - (vc.x - cx0), dvy = (v.y - sy) - (vc.y - cy0), dvz = (v.z - sz) - (vc.z - cz0);
-        double tx = dry * dvz - drz * dvy, ty = drz * dvx - drx * dvz, tz = drx * dvy - dry * dvx;
-        double ax = -drx * drz, ay = -dry * drz, az = (drx * drx + dry * dry);
-        tx = tx + cp.Omega * ax; ty = ty + cp.Omega * ay; tz = tz + cp.Omega * az;
-        jx = jx + p.w * tx; jy = jy + p.w * ty; jz = jz + p.w * tz;
+    const double4_32a c = ct.com[s], vc = ct.vcom[s];
+    double acc = 0;
+    for (uint32_t base = 0; base < m; base += 32) {
+        const uint32_t k = base + lane;
+        if (k < m) {
+            uint32_t i = P.idx[o + k];
+            double4_32a p = pos[i], v = vel[i];
+            double drx = p.x - c.x, dry = p.y - c.y, drz = p.z - c.z;
+            double sx = 0. * p.x, sy = cp.shear * p.x, sz = 0. * p.x;
+            double cx0 = 0. * c.x, cy0 = cp.shear * c.x, cz0 = 0. * c.x;
+            double dvx = (v.x - sx) - (vc.x - cx0), dvy = (v.y - sy) - (vc.y - cy0), dvz = (v.z - sz) - (vc.z - cz0);
+            double tx = dry * dvz - drz * dvy, ty = drz * dvx - drx * dvz, tz = drx * dvy - dry * dvx;
+            double ax = -drx * drz, ay = -dry * drz, az = (drx * drx + dry * dry);
+            tx = tx + cp.Omega * ax;
+            ty = ty + cp.Omega * ay;
+            tz = tz + cp.Omega * az;
+            tile[wid][0][lane] = p.w * tx;
+            tile[wid][1][lane] = p.w * ty;
+            tile[wid][2][lane] = p.w * tz;
+        }
+        __syncwarp();
+        const uint32_t cnt = min(32u, m - base);
+        if (lane < 3)
+            for (uint32_t j = 0; j < cnt; ++j) acc = acc + tile[wid][lane][j];
+        __syncwarp();
     }
-    ct.J[s] = make_double4_32a(jx, jy, jz, 0);
+    double jx = __shfl_sync(0xffffffffu, acc, 0), jy = __shfl_sync(0xffffffffu, acc, 1), jz = __shfl_sync(0xffffffffu, acc, 2);
+    if (lane == 0) ct.J[s] = make_double4_32a(jx, jy, jz, 0);
 }
 
 // copy every live segment into the other pool buffer at packed offsets
@@ -1032,8 +1196,8 @@ struct Stage {
         if (list.empty()) return kOk;
         int rc = up_list(list, d_list);
         if (rc) return rc;
-        k_kinematics<<<grid_for(list.size(), 64), 64, 0, s>>>(d_list, (uint32_t)list.size(), ct, P, tr.pos, tr.vel, with_hill ? 1 : 0, cp.G,
-                                                               cp.Omega);
+        k_kinematics<<<(unsigned)((list.size() + 3) / 4), 128, 0, s>>>(d_list, (uint32_t)list.size(), ct, P, tr.pos, tr.vel, with_hill ? 1 : 0,
+                                                                        cp.G, cp.Omega);
         c.launches++;
         PLAN_CUDA(cudaGetLastError());
         return kOk;
@@ -1106,7 +1270,7 @@ struct Stage {
         if (list.empty()) return kOk;
         int rc = up_list(list, d_list);
         if (rc) return rc;
-        k_dispersion<<<grid_for(list.size(), 64), 64, 0, s>>>(d_list, (uint32_t)list.size(), ct, P, tol, d_flag8);
+        k_dispersion<<<(unsigned)((list.size() + 3) / 4), 128, 0, s>>>(d_list, (uint32_t)list.size(), ct, P, tol, d_flag8);
         c.launches++;
         return down(res, d_flag8, list.size());
     }
@@ -1170,10 +1334,35 @@ static double wall_ms() {
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
+// PLAN_TRACE=1 in the environment prints the progress of FindPlanetesimals to stderr (the
+// stream is synchronised at every mark, so traced runs are slower; off by default).
+struct Trace {
+    bool on = false;
+    cudaStream_t s = nullptr;
+    double t0 = 0, last = 0;
+    Trace(cudaStream_t st) : s(st) {
+        const char *e = std::getenv("PLAN_TRACE");
+        on = e && *e && *e != '0';
+        t0 = last = wall_ms();
+    }
+    void mark(const char *what, long long a = -1, long long b = -1, long long c = -1) {
+        if (!on) return;
+        cudaStreamSynchronize(s);
+        double t = wall_ms();
+        std::fprintf(stderr, "[plan] %10.1f ms  +%9.1f ms  %s", t - t0, t - last, what);
+        if (a >= 0) std::fprintf(stderr, " %lld", a);
+        if (b >= 0) std::fprintf(stderr, " %lld", b);
+        if (c >= 0) std::fprintf(stderr, " %lld", c);
+        std::fprintf(stderr, "\n");
+        last = t;
+    }
+};
+
 int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogue **out) {
     cudaEvent_t ev[6];
     for (auto &e : ev) cudaEventCreate(&e);
     cudaEventRecord(ev[0], s);
+    Trace trace(s);
     const DevTree &tr = c.tree;
     const uint32_t Tu = tr.Tu, N = c.n_input;
     // kernel choice and thresholds (src/tree.hpp:3576-3660), host scalars
@@ -1210,15 +1399,18 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
     uint32_t *densest = c.arena.get<uint32_t>(Tu);
     if (!densest) return kErrOutOfMemory;
     c.densest = densest;
+    trace.mark("density", c.counters[17]);
     rc = launch_densest(c, p, p.hop, thr, densest, s);
     if (rc) return rc;
     cudaEventRecord(ev[2], s);
+    trace.mark("densest", c.counters[18]);
     // 3. HOP groups
     HopGroups hg;
     rc = hop_groups(c, densest, thr, hg, s);
     if (rc) return rc;
     c.peak = hg.peak;
     cudaEventRecord(ev[3], s);
+    trace.mark("hop groups", hg.n_groups, hg.n_members);
 
     // ------------------------------------------------------------------ clump stage
     Stage st(c, s);
@@ -1275,6 +1467,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
     // SortParticles + the diffuse cut after HOP (src/tree.hpp:3816-3829)
     rc = st.sort_particles(all);
     if (rc) return rc;
+    trace.mark("sort particles of all groups", C);
     std::vector<uint8_t> too;
     std::vector<uint32_t> del_keys_host;
     if (diffuse < 0.525) {
@@ -1456,6 +1649,8 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
             }
             num_planetesimals = (uint32_t)live.size() - delete_count;
             (hill_mode ? c.counters[12] : c.counters[11])++;
+            trace.mark(hill_mode ? "hill merge sweep (sweep, pairs, deleted)" : "merge sweep (sweep, pairs, deleted)", sweep, npairs,
+                       delete_count);
             rc = st.maybe_compact();
             if (rc) return rc;
         }
@@ -1513,8 +1708,10 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
         if (rc) return rc;
     }
     // 5. unbind, mark, rebind (src/tree.hpp:4189-4208)
+    trace.mark("re-key", live.size());
     rc = st.unbind(live);  // includes SortParticles and the Hill radius
     if (rc) return rc;
+    trace.mark("unbind");
     PLAN_CUDA(cudaStreamSynchronize(s));
     double tw2 = wall_ms();
     PLAN_CUDA(cudaMemsetAsync(in_clump, 0, Tu, s));
@@ -1523,6 +1720,24 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
         c.launches++;
     }
     {
+        // the call-independent candidate list E and its prefix counts
+        uint32_t *epos = A.get<uint32_t>((size_t)Tu + 1), *E = A.get<uint32_t>((size_t)Tu + 1);
+        if (A.failed) return kErrOutOfMemory;
+        {
+            Arena &S = c.scratch;
+            size_t mark = S.used;
+            size_t sb = scan_u32_scratch_bytes((size_t)Tu + 1);
+            void *scr = S.take(sb);
+            if (S.failed || !scr) { S.used = mark; return kErrOutOfMemory; }
+            PLAN_CUDA(cudaMemsetAsync(epos + Tu, 0, 4, s));
+            k_elig_flags<<<grid_for(Tu, 256), 256, 0, s>>>(Tu, in_clump, tr.dens, st.cp.thr, epos);
+            rc = scan_u32(epos, epos, (size_t)Tu + 1, nullptr, scr, sb, s);
+            S.used = mark;
+            if (rc) return rc;
+            k_elig_compact<<<grid_for(Tu, 256), 256, 0, s>>>(Tu, in_clump, tr.dens, st.cp.thr, epos, E);
+            c.launches += 4;
+            PLAN_CUDA(cudaGetLastError());
+        }
         // Clumps rebind concurrently (one SearchBound call per clump per round) under the
         // ordered-claim rule of k_rebind_round; passes rerun invalid clumps from their saved
         // state until the result equals the reference's clump-by-clump run in key order.
@@ -1532,6 +1747,8 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
         double4_32a *bc = A.get<double4_32a>(nb), *bv = A.get<double4_32a>(nb);
         uint32_t *bo = A.get<uint32_t>(nb), *bn = A.get<uint32_t>(nb), *owner = A.get<uint32_t>(Tu);
         uint32_t *rank_of = A.get<uint32_t>(nb), *slot_of_rank = A.get<uint32_t>(nb), *dmax = A.get<uint32_t>(nb);
+        uint32_t *dset = A.get<uint32_t>(nb * kDeferSlots);
+        uint8_t *dover = A.get<uint8_t>(nb);
         uint8_t *d_grew = A.get<uint8_t>(nb), *invalid = A.get<uint8_t>(nb), *rerun_rank = A.get<uint8_t>(nb);
         uint32_t *d_mnout = A.get<uint32_t>(nb);
         if (A.failed) return kErrOutOfMemory;
@@ -1567,6 +1784,8 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
         PLAN_CUDA(cudaMemsetAsync(owner, 0xff, (size_t)Tu * 4, s));
         PLAN_CUDA(cudaMemsetAsync(invalid, 0, nb, s));
         PLAN_CUDA(cudaMemsetAsync(dmax, 0, nb * 4, s));
+        PLAN_CUDA(cudaMemsetAsync(dset, 0xff, nb * kDeferSlots * 4, s));
+        PLAN_CUDA(cudaMemsetAsync(dover, 0, nb, s));
         KTree kt = ktree_of(tr);
         uint64_t rounds = 0, passes = 0, reruns = 0;
         auto run_rounds = [&](std::vector<uint32_t> active, int seq_mode) -> int {
@@ -1576,8 +1795,10 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                 int r = st.up_list(active, st.d_list);
                 if (r) return r;
                 double t_a = wall_ms();
-                k_rebind_round<<<(unsigned)active.size(), 256, 0, s>>>(st.d_list, ct, P, kt, tr.vel, tr.dens, in_clump, owner, rank_of,
-                                                                       slot_of_rank, invalid, dmax, seq_mode, st.cp, d_grew, d_mnout, c.d_err);
+                k_rebind_round<<<(unsigned)active.size(), kRebindThreads, 0, s>>>(st.d_list, ct, P, kt, tr.vel, E, epos, in_clump, owner,
+                                                                                  rank_of, slot_of_rank, invalid, dmax, dset, dover, seq_mode,
+                                                                                  st.cp, d_grew,
+                                                                                  d_mnout, c.d_err);
                 c.launches++;
                 PLAN_CUDA(cudaGetLastError());
                 std::vector<uint8_t> g;
@@ -1602,6 +1823,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                 uint64_t mx = 0;
                 for (uint32_t v : grown_mn) mx = std::max<uint64_t>(mx, v);
                 c.counters[16] = std::max<uint64_t>(c.counters[16], mx);
+                if (round % 25 == 0) trace.mark("rebinding round (round, grown, largest)", round, grown.size(), mx);
                 active.swap(grown);
             }
             return kOk;
@@ -1612,19 +1834,32 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
             ++passes;
             rc = run_rounds(active, 0);
             if (rc) return rc;
-            std::vector<uint8_t> inv;
-            std::vector<uint32_t> dm;
+            std::vector<uint8_t> inv, dov;
+            std::vector<uint32_t> dm, ds;
             rc = st.down(inv, invalid, C);
             if (!rc) rc = st.down(dm, dmax, C);
+            if (!rc) rc = st.down(ds, dset, (size_t)C * kDeferSlots);
+            if (!rc) rc = st.down(dov, dover, C);
             if (rc) return rc;
             uint32_t rstar = kNone;
             for (uint32_t r = 0; r < nlive; ++r) if (inv[live[r]]) { rstar = r; break; }
             if (rstar == kNone) break;
+            // rerun the invalid clumps and, in rank order, every clump that skipped particles
+            // of a clump being rerun (its holdings may change); the rest keep their result
             std::vector<uint32_t> rerun;
             std::vector<uint8_t> rr(nlive + 1, 0);
             for (uint32_t r = rstar; r < nlive; ++r) {
                 uint32_t sl = live[r];
-                if (inv[sl] || (dm[sl] && dm[sl] - 1 >= rstar)) { rerun.push_back(sl); rr[r] = 1; }
+                bool again = inv[sl] != 0;
+                if (!again && dov[sl]) {
+                    again = dm[sl] && dm[sl] - 1 >= rstar;
+                } else if (!again) {
+                    for (int j = 0; j < kDeferSlots && !again; ++j) {
+                        uint32_t d = ds[(size_t)sl * kDeferSlots + j];
+                        again = d != kNone && d >= rstar && d < nlive && rr[d];
+                    }
+                }
+                if (again) { rerun.push_back(sl); rr[r] = 1; }
             }
             reruns += rerun.size();
             PLAN_CUDA(cudaMemcpyAsync(rerun_rank, rr.data(), nlive, cudaMemcpyHostToDevice, s));
@@ -1632,7 +1867,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
             rc = st.up_list(rerun, st.d_list2);
             if (rc) return rc;
             k_rebind_restore<<<(unsigned)rerun.size(), 256, 0, s>>>(st.d_list2, (uint32_t)rerun.size(), ct, P, bM, bh, bri, bro, br10, br2,
-                                                                    bc, bv, bo, bn, bidx, bdist, invalid, dmax, c.d_err);
+                                                                    bc, bv, bo, bn, bidx, bdist, invalid, dmax, dset, dover, c.d_err);
             c.launches += 2;
             PLAN_CUDA(cudaGetLastError());
             active = rerun;
@@ -1644,6 +1879,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
     }
     PLAN_CUDA(cudaStreamSynchronize(s));
     double tw3 = wall_ms();
+    trace.mark("rebinding done (rounds, passes, reruns)", c.stage_ms[14], c.counters[12], c.counters[14]);
     // 6. prune and loose streams (src/tree.hpp:4213-4224)
     auto prune = [&]() -> int {
         if (!C) return kOk;
@@ -1716,12 +1952,13 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
     if (!live.empty()) {
         rc = st.up_list(live, st.d_list);
         if (rc) return rc;
-        k_angmom<<<grid_for(live.size(), 64), 64, 0, s>>>(st.d_list, (uint32_t)live.size(), ct, P, tr.pos, tr.vel, st.cp);
+        k_angmom<<<(unsigned)((live.size() + 3) / 4), 128, 0, s>>>(st.d_list, (uint32_t)live.size(), ct, P, tr.pos, tr.vel, st.cp);
         c.launches++;
     }
     cudaEventRecord(ev[5], s);
     PLAN_CUDA(cudaStreamSynchronize(s));
     double tw4 = wall_ms();
+    trace.mark("prune, rip, ghost cut, J");
     c.stage_ms[10] = tw1 - tw0;  // HOP-group sort + both merge sweeps
     c.stage_ms[11] = tw2 - tw1;  // re-key + unbinding
     c.stage_ms[12] = tw3 - tw2;  // Hill rebinding
@@ -1749,6 +1986,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
     std::vector<uint32_t> base(nl + 1, 0);
     for (uint32_t t = 0; t < nl; ++t) base[t + 1] = base[t] + mn[live[t]];
     const uint32_t tot = base[nl];
+    uint64_t d2h = (uint64_t)C * (4 + 4 + 8 + 3 * 32);  // catalogue bytes read back: clump table ...
     if (nl) {
         uint32_t *dl = A.get<uint32_t>(nl), *db = A.get<uint32_t>(nl + 1), *ocnt = A.get<uint32_t>(tot + 1), *obase = A.get<uint32_t>(tot + 1);
         uint32_t *d_otot = A.get<uint32_t>(2);
@@ -1783,6 +2021,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
         if (!rc) rc = st.down(hopos, opos, 3 * (size_t)otot);
         if (!rc) rc = st.down(hob, obase, tot);
         if (rc) { delete cat; return rc; }
+        d2h += 4 + (uint64_t)tot * (24 + 24 + 8 + 4 + 4) + (uint64_t)otot * 24;  // ... and member records
         cat->clumps.resize(nl);
         for (uint32_t t = 0; t < nl; ++t) {
             uint32_t sl = live[t];
@@ -1803,6 +2042,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
         }
         cat->have_members = true;
     }
+    trace.mark("catalogue download");
     finish_catalogue(*cat, p.num_peaks);  // ranking, cap, host-libm values, summary
     rc = st.sync();
     if (rc) { delete cat; return rc; }
@@ -1814,6 +2054,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
     c.stage_ms[8] = wall_ms() - tw4;  // catalogue download and host finishing
     for (auto &e : ev) cudaEventDestroy(e);
     c.counters[7] = cat->clumps.size();
+    c.counters[21] = d2h;
     if (out) *out = cat;
     else delete cat;
     return kOk;

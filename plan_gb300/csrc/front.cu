@@ -466,6 +466,24 @@ int build_octree(Context &c, double4_32a *in_pos, double4_32a *in_vel, const uin
     PLAN_CUDA(cudaMemcpyAsync(&Tu, d_tot, 4, cudaMemcpyDeviceToHost, s));
     PLAN_CUDA(cudaStreamSynchronize(s));
     c.launches += 5;
+    if (Tu < T) {
+        // Repeated keys: which particle represents a sink, and the order its velocities are
+        // summed in, follow the library sort's order of equal keys. Redo the sort from the
+        // input order with the introsort of the library; the runs (and Tu) are unchanged.
+        if (mass_table) {
+            k_keys<<<grid_for(T, 256), 256, 0, s>>>(in_pos, in_type, T, box, mt, kw0, kw1, kw2, kidx, c.d_err);
+        } else {
+            k_keys_keep_mass<<<grid_for(T, 256), 256, 0, s>>>(in_pos, T, box, kw0, kw1, kw2, kidx);
+        }
+        c.launches++;
+        const size_t mb = morton_sort_scratch_bytes(T);
+        void *ms = nullptr;
+        PLAN_CUDA(cudaMallocAsync(&ms, mb, s));
+        rc = morton_sort_std(c, kw0, kw1, kw2, kidx, T, ms, mb, s);
+        cudaFreeAsync(ms, s);
+        if (rc) return rc;
+        c.counters[19] += 1;  // sorts that took the library order of equal keys
+    }
     tr = DevTree();
     tr.T = T;
     tr.Tu = Tu;
@@ -586,13 +604,23 @@ int build_tree(Context &c, const plan_lis_view &v, plan_params &p, int first_fil
     void *scrA = S.take(sortA);
     if (S.failed) return kErrOutOfMemory;
 
-    // 1. upload and unpack
-    size_t at = 0;
-    for (uint32_t b = 0; b < v.nblocks; ++b) {
-        PLAN_CUDA(cudaMemcpyAsync(d_rec + at * 44, v.records[b], v.counts[b] * 44, cudaMemcpyHostToDevice, s));
-        at += v.counts[b];
+    // 1. upload and unpack; a single block already in device memory is read in place
+    const unsigned char *src = d_rec;
+    cudaPointerAttributes pa{};
+    if (v.nblocks == 1 && cudaPointerGetAttributes(&pa, v.records[0]) == cudaSuccess && pa.type == cudaMemoryTypeDevice &&
+        pa.device == c.device) {
+        src = static_cast<const unsigned char *>(v.records[0]);
+        c.counters[20] = 0;
+    } else {
+        cudaGetLastError();
+        size_t at = 0;
+        for (uint32_t b = 0; b < v.nblocks; ++b) {
+            PLAN_CUDA(cudaMemcpyAsync(d_rec + at * 44, v.records[b], v.counts[b] * 44, cudaMemcpyDefault, s));
+            at += v.counts[b];
+        }
+        c.counters[20] = (uint64_t)N * 44;  // bytes uploaded
     }
-    k_unpack<<<grid_for(N, 256), 256, 0, s>>>(d_rec, N, tmp_pos, tmp_vel, tmp_type, aw0, aw1, aw2, aidx);
+    k_unpack<<<grid_for(N, 256), 256, 0, s>>>(src, N, tmp_pos, tmp_vel, tmp_type, aw0, aw1, aw2, aidx);
     PLAN_CUDA(cudaMemsetAsync(d_desc, 0, 32, s));
     k_count_descents<<<grid_for(N, 256), 256, 0, s>>>(aw0, aw1, N, d_desc);
     c.launches += 2;

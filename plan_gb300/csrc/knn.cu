@@ -14,6 +14,7 @@
 
 #include "pipeline.h"
 #include "tree_walk.cuh"
+#include "knn_f32.cuh"
 
 namespace plan {
 
@@ -98,6 +99,137 @@ __global__ void __launch_bounds__(128) k_density_at(KTree t, const double *q3, c
     out[i] = got == (int)k ? knn_median_density(t, h, (int)k, four_pi_over_three) : 0.0;
 }
 
+// ---------------------------------------------------------------- FP32-filtered kernels
+__global__ void k_split_points(const double4_32a *pos, uint32_t n, float4 *hi, float4 *lo) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double4_32a p = pos[i];
+    float hx = (float)p.x, hy = (float)p.y, hz = (float)p.z;
+    hi[i] = make_float4(hx, hy, hz, 0.f);
+    lo[i] = make_float4((float)(p.x - (double)hx), (float)(p.y - (double)hy), (float)(p.z - (double)hz), 0.f);
+}
+
+__global__ void k_split_nodes(const double4_32a *ncf, uint32_t n, float4 *hi, float4 *lo) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double4_32a c = ncf[i];
+    float hx = (float)c.x, hy = (float)c.y, hz = (float)c.z, hw = (float)c.w;
+    hi[i] = make_float4(hx, hy, hz, hw);
+    lo[i] = make_float4((float)(c.x - (double)hx), (float)(c.y - (double)hy), (float)(c.z - (double)hz), (float)(c.w - (double)hw));
+}
+
+__device__ __forceinline__ double f_median_density(const KTree &t, const double *d64, const uint32_t *i64, int k, double fpo3) {
+    int i = k;
+    double m2 = 4 * d64[i / 2];
+    for (i = i - 1; i >= 0; i--) {
+        if (d64[i] > m2) continue;
+        break;
+    }
+    double r2 = d64[i];
+    double dens = 0;
+    for (; i >= 0; i--) dens = dens + t.pos[i64[i]].w;
+    return dens / (fpo3 * cr_pow15(r2));
+}
+
+template <int CAP>
+__global__ void __launch_bounds__(128) k_density_f(KTree t, FTree f, uint32_t n, uint32_t k, double fpo3, double *dens, uint32_t *redo,
+                                                   uint32_t *nredo, unsigned *err) {
+    extern __shared__ unsigned char smem[];
+    float *sk = reinterpret_cast<float *>(smem);
+    uint32_t *si = reinterpret_cast<uint32_t *>(sk + CAP * blockDim.x);
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    FHeap fh{sk + threadIdx.x, si + threadIdx.x, (int)blockDim.x};
+    double d64[CAP];
+    uint32_t i64[CAP];
+    double4_32a q = t.pos[i];
+    double r = knn_first_radius(t, q.x, q.y, q.z, t.leaf_of[i], k, err);
+    int got = knn_query_f32(t, f, i, q.x, q.y, q.z, r, k, CAP, fh, d64, i64, err);
+    if (got < 0) {
+        redo[atomicAdd(nredo, 1u)] = i;
+        return;
+    }
+    dens[i] = f_median_density(t, d64, i64, (int)k, fpo3);
+}
+
+template <int CAP>
+__global__ void __launch_bounds__(128) k_densest_f(KTree t, FTree f, uint32_t n, uint32_t k, double threshold, const double *dens,
+                                                   uint32_t *densest, uint32_t *redo, uint32_t *nredo, unsigned *err) {
+    extern __shared__ unsigned char smem[];
+    float *sk = reinterpret_cast<float *>(smem);
+    uint32_t *si = reinterpret_cast<uint32_t *>(sk + CAP * blockDim.x);
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double di = dens[i];
+    uint32_t best = i;
+    if (di >= threshold) {  // src/tree.hpp:3719-3735
+        FHeap fh{sk + threadIdx.x, si + threadIdx.x, (int)blockDim.x};
+        double d64[CAP];
+        uint32_t i64[CAP];
+        double4_32a q = t.pos[i];
+        double r = knn_first_radius(t, q.x, q.y, q.z, t.leaf_of[i], k, err);
+        int got = knn_query_f32(t, f, i, q.x, q.y, q.z, r, k, CAP, fh, d64, i64, err);
+        if (got < 0) {
+            redo[atomicAdd(nredo, 1u)] = i;
+            return;
+        }
+        double bd = di;
+        for (int j = 0; j < got; ++j) {
+            uint32_t c = i64[j];
+            double dc = dens[c];
+            if (bd < dc) { best = c; bd = dc; }
+            else if (bd == dc && best > c) best = c;
+        }
+    }
+    densest[i] = best;
+}
+
+// exact FP64 path for a list of queries
+template <int KMAX>
+__global__ void __launch_bounds__(128) k_density_list(KTree t, const uint32_t *list, uint32_t n, uint32_t k, double fpo3, double *dens,
+                                                      unsigned *err) {
+    extern __shared__ unsigned char smem[];
+    double *sd = reinterpret_cast<double *>(smem);
+    uint32_t *si = reinterpret_cast<uint32_t *>(sd + KMAX * blockDim.x);
+    uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    uint32_t i = list[j];
+    SlabHeap h{sd + threadIdx.x, si + threadIdx.x, (int)blockDim.x};
+    double4_32a q = t.pos[i];
+    double r = knn_first_radius(t, q.x, q.y, q.z, t.leaf_of[i], k, err);
+    int got = knn_query(t, q.x, q.y, q.z, r, k, h, err);
+    if (got < (int)k) {
+        atomicOr(err, (unsigned)kDevErrCapacity);
+        dens[i] = 0;
+        return;
+    }
+    dens[i] = knn_median_density(t, h, (int)k, fpo3);
+}
+
+template <int KMAX>
+__global__ void __launch_bounds__(128) k_densest_list(KTree t, const uint32_t *list, uint32_t n, uint32_t k, double threshold,
+                                                      const double *dens, uint32_t *densest, unsigned *err) {
+    extern __shared__ unsigned char smem[];
+    double *sd = reinterpret_cast<double *>(smem);
+    uint32_t *si = reinterpret_cast<uint32_t *>(sd + KMAX * blockDim.x);
+    uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    uint32_t i = list[j];
+    SlabHeap h{sd + threadIdx.x, si + threadIdx.x, (int)blockDim.x};
+    double4_32a q = t.pos[i];
+    double r = knn_first_radius(t, q.x, q.y, q.z, t.leaf_of[i], k, err);
+    int got = knn_query(t, q.x, q.y, q.z, r, k, h, err);
+    uint32_t best = i;
+    double bd = dens[i];
+    for (int jj = 0; jj < got; ++jj) {
+        uint32_t c = h.iget(jj);
+        double dc = dens[c];
+        if (bd < dc) { best = c; bd = dc; }
+        else if (bd == dc && best > c) best = c;
+    }
+    densest[i] = best;
+}
+
 template <class F>
 int launch_by_k(uint32_t k, F f) {
     if (k <= 32) return f(std::integral_constant<int, 32>(), 128);
@@ -108,13 +240,64 @@ int launch_by_k(uint32_t k, F f) {
 
 }  // namespace
 
+// FP32 hi/lo copies of points and node centres for the filtered kernels
+static int ensure_split(Context &c, cudaStream_t s) {
+    DevTree &tr = c.tree;
+    if (tr.phi) return kOk;
+    tr.phi = c.arena.get<float4>(tr.Tu);
+    tr.plo = c.arena.get<float4>(tr.Tu);
+    tr.nhi = c.arena.get<float4>(tr.nodes);
+    tr.nlo = c.arena.get<float4>(tr.nodes);
+    if (c.arena.failed) return kErrOutOfMemory;
+    k_split_points<<<grid_for(tr.Tu, 256), 256, 0, s>>>(tr.pos, tr.Tu, tr.phi, tr.plo);
+    k_split_nodes<<<grid_for(tr.nodes, 256), 256, 0, s>>>(tr.ncf, tr.nodes, tr.nhi, tr.nlo);
+    c.launches += 2;
+    PLAN_CUDA(cudaGetLastError());
+    return kOk;
+}
+
+template <class F>
+static int launch_by_cap(uint32_t k, F f) {
+    if (k <= 16) return f(std::integral_constant<int, 24>());
+    if (k <= 32) return f(std::integral_constant<int, 40>());
+    if (k <= 64) return f(std::integral_constant<int, 72>());
+    return kErrUnsupported;
+}
+
 int launch_density(Context &c, const plan_params &p, uint32_t k, cudaStream_t s) {
     KTree t = ktree_of(c.tree);
     const double fpo3 = 3.14159265358979323846 * 4. / 3.;
+    int rc = ensure_split(c, s);
+    if (rc) return rc;
+    FTree f{c.tree.phi, c.tree.plo, c.tree.nhi, c.tree.nlo};
+    const uint32_t n = c.tree.Tu;
+    uint32_t *redo = c.scratch.get<uint32_t>(n + 1), *nredo = c.scratch.get<uint32_t>(4);
+    if (!redo || !nredo) return kErrOutOfMemory;
+    PLAN_CUDA(cudaMemsetAsync(nredo, 0, 4, s));
+    rc = launch_by_cap(k, [&](auto capc) {
+        constexpr int CAP = decltype(capc)::value;
+        size_t sm = (size_t)CAP * 128 * 8;
+        if (sm > 48 * 1024) PLAN_CUDA(cudaFuncSetAttribute(k_density_f<CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        PLAN_CUDA(cudaEventRecord(c.kev[0], s));
+        k_density_f<CAP><<<grid_for(n, 128), 128, sm, s>>>(t, f, n, k, fpo3, c.tree.dens, redo, nredo, c.d_err);
+        PLAN_CUDA(cudaEventRecord(c.kev[1], s));
+        c.launches++;
+        PLAN_CUDA(cudaGetLastError());
+        return (int)kOk;
+    });
+    if (rc) return rc;
+    uint32_t h = 0;
+    PLAN_CUDA(cudaMemcpyAsync(&h, nredo, 4, cudaMemcpyDeviceToHost, s));
+    PLAN_CUDA(cudaStreamSynchronize(s));
+    float kms = 0;
+    cudaEventElapsedTime(&kms, c.kev[0], c.kev[1]);
+    c.stage_ms[20] = kms;  // the FP32-filtered density kernel alone
+    c.counters[17] = h;
+    if (!h) return kOk;
     return launch_by_k(k, [&](auto km, int threads) {
         constexpr int KM = decltype(km)::value;
         size_t sm = (size_t)KM * threads * 12;
-        k_density<KM><<<grid_for(c.tree.Tu, threads), threads, sm, s>>>(t, c.tree.Tu, k, fpo3, c.tree.dens, c.d_err);
+        k_density_list<KM><<<grid_for(h, threads), threads, sm, s>>>(t, redo, h, k, fpo3, c.tree.dens, c.d_err);
         c.launches++;
         PLAN_CUDA(cudaGetLastError());
         return (int)kOk;
@@ -123,10 +306,37 @@ int launch_density(Context &c, const plan_params &p, uint32_t k, cudaStream_t s)
 
 int launch_densest(Context &c, const plan_params &p, uint32_t k, double threshold, uint32_t *densest, cudaStream_t s) {
     KTree t = ktree_of(c.tree);
+    int rc = ensure_split(c, s);
+    if (rc) return rc;
+    FTree f{c.tree.phi, c.tree.plo, c.tree.nhi, c.tree.nlo};
+    const uint32_t n = c.tree.Tu;
+    uint32_t *redo = c.scratch.get<uint32_t>(n + 1), *nredo = c.scratch.get<uint32_t>(4);
+    if (!redo || !nredo) return kErrOutOfMemory;
+    PLAN_CUDA(cudaMemsetAsync(nredo, 0, 4, s));
+    rc = launch_by_cap(k, [&](auto capc) {
+        constexpr int CAP = decltype(capc)::value;
+        size_t sm = (size_t)CAP * 128 * 8;
+        if (sm > 48 * 1024) PLAN_CUDA(cudaFuncSetAttribute(k_densest_f<CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        PLAN_CUDA(cudaEventRecord(c.kev[0], s));
+        k_densest_f<CAP><<<grid_for(n, 128), 128, sm, s>>>(t, f, n, k, threshold, c.tree.dens, densest, redo, nredo, c.d_err);
+        PLAN_CUDA(cudaEventRecord(c.kev[1], s));
+        c.launches++;
+        PLAN_CUDA(cudaGetLastError());
+        return (int)kOk;
+    });
+    if (rc) return rc;
+    uint32_t h = 0;
+    PLAN_CUDA(cudaMemcpyAsync(&h, nredo, 4, cudaMemcpyDeviceToHost, s));
+    PLAN_CUDA(cudaStreamSynchronize(s));
+    float kms = 0;
+    cudaEventElapsedTime(&kms, c.kev[0], c.kev[1]);
+    c.stage_ms[21] = kms;  // the FP32-filtered densest-neighbour kernel alone
+    c.counters[18] = h;
+    if (!h) return kOk;
     return launch_by_k(k, [&](auto km, int threads) {
         constexpr int KM = decltype(km)::value;
         size_t sm = (size_t)KM * threads * 12;
-        k_densest<KM><<<grid_for(c.tree.Tu, threads), threads, sm, s>>>(t, c.tree.Tu, k, threshold, c.tree.dens, densest, c.d_err);
+        k_densest_list<KM><<<grid_for(h, threads), threads, sm, s>>>(t, redo, h, k, threshold, c.tree.dens, densest, c.d_err);
         c.launches++;
         PLAN_CUDA(cudaGetLastError());
         return (int)kOk;

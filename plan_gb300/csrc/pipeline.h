@@ -57,6 +57,7 @@ struct DevTree {
     double4_32a *ncf = nullptr;
     uint32_t *nbeg = nullptr, *nend = nullptr, *npar = nullptr, *nfd = nullptr;
     uint8_t *nnd = nullptr, *north = nullptr, *nlev = nullptr;
+    float4 *phi = nullptr, *plo = nullptr, *nhi = nullptr, *nlo = nullptr;  // FP32 hi/lo copies
 };
 
 // Host-visible scalars of a finder run.
@@ -83,6 +84,7 @@ struct Context {
     double time = 0;
     FindScalars fs{};
     uint32_t *densest = nullptr, *peak = nullptr;  // stage arrays of the last finder run
+    cudaEvent_t kev[2] = {nullptr, nullptr};        // brackets one kernel for its timing
     int status_from(int rc, const char *what);
     // grow an arena (contents are discarded) to at least `bytes`
     int ensure(Arena &a, size_t bytes);

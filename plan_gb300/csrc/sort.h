@@ -21,4 +21,12 @@ int radix_sort96(uint32_t *w0, uint32_t *w1, uint32_t *w2, uint32_t *payload, si
 size_t scan_u32_scratch_bytes(size_t n);
 int scan_u32(const uint32_t *in, uint32_t *out, size_t n, uint32_t *d_total, void *scratch, size_t scratch_bytes, cudaStream_t stream);
 
+// The exact arrangement std::sort (libstdc++ introsort) gives 96-bit keys in input order
+// (w0..w2 low word first, ix the payload), in place; used when keys repeat, where the
+// order of equal keys is the library's and not a stable one. Scratch: see below.
+struct Context;
+size_t morton_sort_scratch_bytes(size_t n);
+int morton_sort_std(Context &c, uint32_t *w0, uint32_t *w1, uint32_t *w2, uint32_t *ix, uint32_t n, void *scratch, size_t bytes,
+                    cudaStream_t stream);
+
 }  // namespace plan

@@ -1,0 +1,150 @@
+"""Write the golden fixtures of the parity tests from the reference itself.
+
+For every case of tests/cases.py this script builds the snapshot, runs the UNMODIFIED
+reference (oracle/_ref/plan_ref, compiled from the reference checkout by `make -C oracle
+ref`) with its stage dump switched on, and stores under tests/golden/<case>/:
+
+  meta.json        SHA-256 of the .lis files, the parameters, the reference's summary line,
+                   sizes, and canonical digests of its Morton keys, tree points, node table,
+                   densities, densest-neighbour pointers, clumps and (strided) KNN lists
+  peaks_at_*.txt   the reference's clump catalogue, byte for byte
+  planetesimals.txt  the reference's basic-results file
+  (the per-clump member lists of --Save_Clumps are pinned by their SHA-256 in meta.json)
+
+Run it in a checkout where the reference is present:  python tests/golden/make_golden.py
+It needs the reference binary and the library's generator; nothing at test time runs it.
+"""
+from __future__ import annotations
+
+import json
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent.parent
+sys.path.insert(0, str(ROOT / "tests"))
+sys.path.insert(0, str(ROOT))
+import cases  # noqa: E402
+
+REF = ROOT / "oracle" / "_ref" / "plan_ref"
+
+
+def read_dumps(d: Path, stride: int) -> dict:
+    t = np.fromfile(d / "tree.bin", dtype=np.uint8)
+    n = int(t[:8].view("<u8")[0])
+    rec = np.dtype([("f", "<f8", 9), ("orig", "<u4"), ("sink", "u1")])
+    assert rec.itemsize == 77
+    tr = t[8:].view(rec)
+    assert len(tr) == n
+    k = np.fromfile(d / "keys.bin", dtype=np.uint8)
+    keys = k[8:].view("<u4").reshape(-1, 3)
+    nb = np.fromfile(d / "nodes.bin", dtype=np.uint8)
+    nn = int(nb[:8].view("<u8")[0])
+    nrec = np.dtype([("f", "<f8", 4), ("u", "<u4", 4), ("orth", "<u2"), ("nd", "u1"), ("lvl", "u1")])
+    assert nrec.itemsize == 52
+    nd = nb[8:].view(nrec)
+    assert len(nd) == nn
+    u7 = np.zeros((nn, 7), dtype=np.uint32)
+    u7[:, :4] = nd["u"]
+    u7[:, 4] = nd["orth"]
+    u7[:, 5] = nd["nd"]
+    u7[:, 6] = nd["lvl"]
+    hop = np.fromfile(d / "hop.bin", dtype=np.uint8)[8:].view("<u4")
+    kb = np.fromfile(d / "knn.bin", dtype=np.uint8)
+    hdr = kb[:12].view("<u4")
+    kd = int(hdr[2])
+    assert int(hdr[1]) == stride
+    kr = kb[12:].view(np.dtype([("i", "<u4"), ("d", "<f8")])).reshape(-1, kd)
+    cb = np.fromfile(d / "clumps.bin", dtype=np.uint8)
+    nc = int(cb[:8].view("<u8")[0])
+    off = 8
+    pn = np.zeros((nc, 2), dtype=np.uint32)
+    f11 = np.zeros((nc, 11))
+    mem = []
+    for c in range(nc):
+        pn[c] = cb[off:off + 8].view("<u4")
+        off += 8
+        f11[c] = cb[off:off + 88].view("<f8")
+        off += 88
+        m = int(pn[c, 1])
+        mem.append(cb[off:off + 4 * m].view("<u4").copy())
+        off += 4 * m
+    assert off == len(cb)
+    members = np.concatenate(mem) if mem else np.zeros(0, dtype=np.uint32)
+    return {
+        "n_tree": n, "n_nodes": nn, "n_clumps": nc, "knn_stride": stride, "knn_k": kd,
+        "keys": cases.digest_keys(keys),
+        "points": cases.digest_points(tr["f"], tr["orig"], tr["sink"]),
+        "density": cases.digest_density(tr["f"][:, 8]),
+        "nodes": cases.digest_nodes(nd["f"], u7),
+        "densest": cases.digest_u32(hop),
+        "clumps": cases.digest_clumps(pn, f11, members),
+        "knn": cases.digest_knn(kr["i"], kr["d"]),
+        "n_sinks": int(tr["sink"].sum()),
+    }
+
+
+def oracle_cr(m: dict) -> dict:
+    """Digests of the oracle restatement run with a correctly rounded pow(x, 1.5), which is
+    what the GPU computes; the reference calls the host libm. The number of densities that
+    differ (each by one unit in the last place) is recorded with them."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+
+    o0 = oracle.Oracle(m["lis"], m["param"], pow_mode=0)
+    o0.find()
+    o1 = oracle.Oracle(m["lis"], m["param"], pow_mode=1)
+    o1.find()
+    d0 = o0.points()[0][:, 8]
+    d1 = o1.points()[0][:, 8]
+    diff = d0 != d1
+    rel = float(np.max(np.abs(d1[diff] - d0[diff]) / np.abs(d0[diff]))) if diff.any() else 0.0
+    return {"density_cr": cases.digest_density(d1), "densest_cr": cases.digest_u32(o1.densest()),
+            "clumps_cr": cases.digest_clumps(*o1.clumps()), "n_density_cr_diff": int(diff.sum()),
+            "max_rel_density_cr_diff": rel}
+
+
+def main() -> None:
+    if not REF.exists():
+        sys.exit(f"{REF} missing: run `make -C oracle ref` in a checkout with the reference")
+    only = set(sys.argv[1:])
+    for c in cases.CASES:
+        if only and c.name not in only:
+            continue
+        with tempfile.TemporaryDirectory() as tmp:
+            tmp = Path(tmp)
+            m = cases.materialise(c, tmp / "in")
+            out = tmp / "ref"
+            out.mkdir()
+            dump = tmp / "dump"
+            dump.mkdir()
+            stride = 1 if c.n <= 100000 else 97
+            env = dict(os.environ, PLAN_REF_DUMP=str(dump), PLAN_REF_KNN_STRIDE=str(stride))
+            r = subprocess.run([str(REF)] + cases.cli_args(m, str(out / "res.txt")) + ["--Save_Clumps"], env=env, cwd=out,
+                               capture_output=True, text=True, check=True)
+            summary = [ln for ln in r.stdout.splitlines() if "Finish clump finding" in ln]
+            assert len(summary) == 1, r.stdout
+            g = HERE / c.name
+            if g.exists():
+                shutil.rmtree(g)
+            g.mkdir()
+            pk = cases.find_peaks_file(out)
+            shutil.copy(pk, g / pk.name)
+            shutil.copy(out / "res_planetesimals.txt", g / "planetesimals.txt")
+            meta = {"case": c.name, "lis_sha256": m["sha256"], "four_pi_G": m["four_pi_G"], "summary": summary[0].strip(),
+                    "peaks_file": pk.name, "parlist": cases.parlist_digests(out)}
+            meta.update(read_dumps(dump, stride))
+            meta.update(oracle_cr(m))
+            (g / "meta.json").write_text(json.dumps(meta, indent=1) + "\n")
+            print(f"{c.name}: {meta['n_tree']} points, {meta['n_nodes']} nodes, {meta['n_clumps']} clumps, "
+                  f"{meta['n_sinks']} sinks | {meta['summary']}")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,163 @@
+"""GPU path against the reference's golden outputs and the oracle (needs a GB300).
+
+Every stage the device computes is compared bit for bit: Morton keys, sorted tree points
+with sinks, the node table, densities (against the oracle with a correctly rounded
+pow(x, 1.5), which differs from the reference's libm pow by at most a few units in the last
+place on a few points per thousand), densest-neighbour pointers, and the final catalogue
+files (peaks_at_*.txt, the basic-results file and every --Save_Clumps member list) byte for
+byte against the reference's own files.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import cases
+from conftest import GOLDEN, ROOT, golden
+
+pytestmark = pytest.mark.gpu
+
+ALL = [c.name for c in cases.CASES]
+
+
+@pytest.fixture(scope="module")
+def pg(built):
+    return built
+
+
+@pytest.fixture(scope="module")
+def finder(pg):
+    f = pg.Finder(0)
+    yield f
+    f.close()
+
+
+def _points(pg, f):
+    pos = f.stage(pg.PLAN_ARR_TREE_POS)
+    vel = f.stage(pg.PLAN_ARR_TREE_VEL)
+    f9 = np.zeros((len(pos), 9))
+    f9[:, 0:3] = pos[:, 0:3]
+    f9[:, 3:6] = vel[:, 0:3]
+    f9[:, 6] = pos[:, 3]
+    f9[:, 7] = vel[:, 3]
+    f9[:, 8] = f.stage(pg.PLAN_ARR_DENSITY)
+    sink = (f.stage(pg.PLAN_ARR_SINK_COUNT) > 1).astype(np.uint8)
+    return f9, f.stage(pg.PLAN_ARR_ORIG_ID), sink
+
+
+@pytest.mark.parametrize("name", ALL)
+def test_stages_and_catalogue(name, pg, finder, case_dir, tmp_path):
+    g = golden(name)
+    m = case_dir(name)
+    p = pg.params(m["param"])
+    snap = pg.Snapshot(m["lis"])
+    cat = finder.find_clumps(snap, p)
+    f9, orig, sink = _points(pg, finder)
+    assert len(f9) == g["n_tree"]
+    assert cases.digest_keys(finder.stage(pg.PLAN_ARR_KEYS)) == g["keys"]
+    assert cases.digest_points(f9, orig, sink) == g["points"]
+    assert cases.digest_nodes(finder.stage(pg.PLAN_ARR_NODE_F), finder.stage(pg.PLAN_ARR_NODE_U)) == g["nodes"]
+    assert cases.digest_density(f9[:, 8]) == g["density_cr"]
+    assert cases.digest_u32(finder.stage(pg.PLAN_ARR_DENSEST)) == g["densest_cr"]
+    assert len(cat) == g["n_clumps"]
+    assert cat.summary().strip() == g["summary"]
+    cat.write_peaks(str(tmp_path / "res.txt"))
+    assert (tmp_path / g["peaks_file"]).read_bytes() == (GOLDEN / name / g["peaks_file"]).read_bytes()
+    line = cat.basic_results(p, with_header=True)
+    assert line == (GOLDEN / name / "planetesimals.txt").read_text()
+    cat.close()
+    snap.close()
+
+
+@pytest.mark.parametrize("name", ["w1_20k", "w1_20k_sinks", "w1_20k_sheared", "w1_24k_split2", "w1_20k_uniform"])
+def test_cli_drop_in(name, pg, case_dir, tmp_path):
+    """The plan_gpu binary with the reference's command line writes the reference's files."""
+    g = golden(name)
+    m = case_dir(name)
+    out = tmp_path / "out"
+    out.mkdir()
+    cli = ROOT / "plan_gb300" / "lib" / "plan_gpu"
+    r = subprocess.run([str(cli)] + cases.cli_args(m, str(out / "res.txt")) + ["--Save_Clumps"], cwd=out, capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert g["summary"] in r.stdout
+    assert (out / g["peaks_file"]).read_bytes() == (GOLDEN / name / g["peaks_file"]).read_bytes()
+    assert (out / "res_planetesimals.txt").read_bytes() == (GOLDEN / name / "planetesimals.txt").read_bytes()
+    assert cases.parlist_digests(out) == g["parlist"]
+
+
+def test_knn_against_oracle(pg, finder, case_dir):
+    """plan_knn (the reference's KNN_Search_OpenMP on arbitrary positions): index sets and
+    squared distances identical to the oracle for tree points, for positions between them
+    with a caller radius (the saddle-point queries of the merge sweeps) and for positions
+    outside the root box. A position without a leaf in the tree is an error on both sides
+    (the reference reports Key2Leaf failing and its KNN is undefined there)."""
+    import oracle
+
+    m = case_dir("w1_20k_sinks")
+    p = pg.params(m["param"])
+    snap = pg.Snapshot(m["lis"])
+    finder.find_clumps(snap, p).close()
+    o = oracle.Oracle(m["lis"], m["param"], threads=1, pow_mode=1)
+    pts = o.points()[0][:, :3]
+    rng = np.random.default_rng(3)
+    tree_q = pts[rng.choice(len(pts), 300, replace=False)]
+    free_q = rng.uniform(-0.1, 0.1, (200, 3))
+    out_q = rng.uniform(0.126, 0.14, (100, 3)) * rng.choice([-1.0, 1.0], (100, 3))
+    for q, k, est in ((tree_q, 32, 0.0), (tree_q, 16, 0.0), (tree_q, 64, 0.0), (free_q, 32, 0.004), (free_q, 7, 0.001),
+                      (out_q, 32, 0.0)):
+        gi, gd = finder.knn(q, k, est)
+        oi, od = o.knn(q, k, est)
+        np.testing.assert_array_equal(gi, oi)
+        np.testing.assert_array_equal(gd, od)
+    n_leafless = 0
+    for x in free_q[:60]:
+        try:
+            oi, od = o.knn(x[None, :], 32, 0.0)
+        except LookupError:
+            n_leafless += 1
+            with pytest.raises(pg.PlanError) as e:
+                finder.knn(x[None, :], 32, 0.0)
+            assert e.value.status == 7
+            continue
+        gi, gd = finder.knn(x[None, :], 32, 0.0)
+        np.testing.assert_array_equal(gi, oi)
+        np.testing.assert_array_equal(gd, od)
+    snap.close()
+
+
+def test_peak_assignment_against_oracle(pg, finder, case_dir):
+    """HOP roots (pointer jumping) against the oracle's chain walk."""
+    import oracle
+
+    m = case_dir("config1_262k")
+    p = pg.params(m["param"])
+    snap = pg.Snapshot(m["lis"])
+    finder.find_clumps(snap, p).close()
+    o = oracle.Oracle(m["lis"], m["param"], threads=os.cpu_count() or 1, pow_mode=1)
+    o.find()
+    np.testing.assert_array_equal(finder.stage(pg.PLAN_ARR_PEAK), o.peaks())
+    snap.close()
+
+
+def test_repeat_runs_identical(pg, case_dir):
+    """Two snapshots through one context, then the first again: identical results (no state
+    leaks between snapshots)."""
+    f = pg.Finder(0)
+    try:
+        out = []
+        for name in ("w1_20k", "w1_20k_border", "w1_20k"):
+            m = case_dir(name)
+            snap = pg.Snapshot(m["lis"])
+            cat = f.find_clumps(snap, pg.params(m["param"]))
+            out.append([tuple(c.items()) for c in map(lambda d: d, cat.clumps())])
+            cat.close()
+            snap.close()
+        assert out[0] == out[2]
+        assert out[0] != out[1]
+    finally:
+        f.close()

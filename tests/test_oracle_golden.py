@@ -1,0 +1,97 @@
+"""The oracle restatement against the reference's own outputs (CPU only).
+
+Golden fixtures come from the unmodified reference run on the same snapshots
+(tests/golden/make_golden.py). These tests pin the oracle before it is trusted to check the
+GPU: every stage digest and both output files must be identical.
+"""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+import pytest
+
+import cases
+from conftest import GOLDEN, golden
+
+CPU_CASES = [c.name for c in cases.CASES]
+
+
+@pytest.fixture(scope="module")
+def oracle_mod(built):
+    from plan_gb300 import build as b
+
+    b.build_oracle()
+    import oracle
+
+    return oracle
+
+
+@pytest.mark.parametrize("name", CPU_CASES)
+def test_snapshot_bytes_pinned(name, case_dir):
+    """The generator and the case edits reproduce the golden snapshot bytes."""
+    m = case_dir(name)
+    assert m["sha256"] == golden(name)["lis_sha256"]
+
+
+@pytest.mark.parametrize("name", CPU_CASES)
+def test_oracle_matches_reference(name, case_dir, oracle_mod, tmp_path):
+    g = golden(name)
+    m = case_dir(name)
+    o = oracle_mod.Oracle(m["lis"], m["param"], threads=os.cpu_count() or 1, pow_mode=0)
+    o.find()
+    f, orig, sink = o.points()
+    assert len(f) == g["n_tree"]
+    assert cases.digest_keys(o.keys()) == g["keys"]
+    assert cases.digest_points(f, orig, sink) == g["points"]
+    assert int(sink.sum()) == g["n_sinks"]
+    assert cases.digest_nodes(*o.nodes()) == g["nodes"]
+    assert cases.digest_density(f[:, 8]) == g["density"]
+    assert cases.digest_u32(o.densest()) == g["densest"]
+    assert cases.digest_clumps(*o.clumps()) == g["clumps"]
+    assert o.summary().strip() == g["summary"]
+    # output files, byte for byte
+    out = tmp_path / "res.txt"
+    o.write_outputs(str(out), first=True)
+    assert (tmp_path / g["peaks_file"]).read_bytes() == (GOLDEN / name / g["peaks_file"]).read_bytes()
+    assert (tmp_path / "res_planetesimals.txt").read_bytes() == (GOLDEN / name / "planetesimals.txt").read_bytes()
+
+
+@pytest.mark.parametrize("name", ["w1_20k", "w1_20k_sinks", "config1_262k"])
+def test_oracle_knn_matches_reference(name, case_dir, oracle_mod):
+    """The approximate KNN (radius doubling, heap order) of every strided query point."""
+    g = golden(name)
+    m = case_dir(name)
+    o = oracle_mod.Oracle(m["lis"], m["param"], threads=1, pow_mode=0)
+    f = o.points()[0]
+    q = f[:: g["knn_stride"], :3]
+    idx, dr2 = o.knn(q, g["knn_k"])
+    assert cases.digest_knn(idx, dr2) == g["knn"]
+
+
+@pytest.mark.parametrize("name", ["w1_20k", "w1_20k_sinks", "config1_262k"])
+def test_oracle_correctly_rounded_pow(name, case_dir, oracle_mod):
+    """With a correctly rounded pow(x, 1.5) (the GPU's) the densities move by at most a few
+    units in the last place and every catalogue digest stays the same."""
+    g = golden(name)
+    m = case_dir(name)
+    o0 = oracle_mod.Oracle(m["lis"], m["param"], pow_mode=0)
+    o0.find()
+    o1 = oracle_mod.Oracle(m["lis"], m["param"], pow_mode=1)
+    o1.find()
+    d0, d1 = o0.points()[0][:, 8], o1.points()[0][:, 8]
+    assert cases.digest_density(d1) == g["density_cr"]
+    rel = np.abs(d1 - d0) / np.abs(d0)
+    assert float(rel.max()) <= 1e-15  # far inside the stated density tolerance of 1e-5 relative
+    assert int((d0 != d1).sum()) == g["n_density_cr_diff"]
+    assert cases.digest_u32(o1.densest()) == g["densest_cr"]
+    assert cases.digest_clumps(*o1.clumps()) == g["clumps"]
+
+
+def test_oracle_morton_order_distinct_keys(oracle_mod):
+    """Without repeats the comparator order is the plain lexicographic key order."""
+    rng = np.random.default_rng(3)
+    k = rng.integers(0, 2**32, size=(5000, 3), dtype=np.uint64).astype(np.uint32)
+    k[:, 2] &= 0xF
+    order = oracle_mod.morton_order(k)
+    np.testing.assert_array_equal(order, np.lexsort((k[:, 0], k[:, 1], k[:, 2])))

@@ -1,0 +1,57 @@
+"""Several GPUs run independent replicas of the path (one snapshot per rank, no data
+exchange): the host-side rules of bench.py checked with two gloo ranks on the CPU."""
+from __future__ import annotations
+
+import os
+import socket
+
+import pytest
+import torch.multiprocessing as mp
+
+
+def _free_port() -> int:
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def _rank(rank: int, world: int, port: int, out):
+    import torch.distributed as dist
+
+    import bench
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    mine = 100.0 + 50.0 * rank  # rank 1 is the slower replica
+    slowest = bench.reduce_max(mine, dist)
+    out.put((rank, bench.replica_seed(rank), slowest, bench.aggregate(world, 1000, 4, slowest)))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_two_replicas_gloo():
+    world = 2
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank, args=(r, world, port, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    got = sorted(q.get(timeout=120) for _ in range(world))
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    seeds = [g[1] for g in got]
+    assert len(set(seeds)) == world  # distinct snapshots per replica
+    for _, _, slowest, value in got:
+        assert slowest == 150.0  # every rank sees the slowest replica's time
+        assert value == pytest.approx(2 * 1000 * 4 / 0.150)
+
+
+def test_single_process_has_no_collective():
+    import bench
+
+    assert bench.reduce_max(7.5, None) == 7.5
+    assert bench.aggregate(1, 10, 2, 1000.0) == 20.0
