@@ -2,6 +2,7 @@
 #include "oracle.hpp"
 
 #include <algorithm>
+#include <chrono>
 #include <cerrno>
 #include <cmath>
 #include <cstdio>
@@ -884,6 +885,15 @@ std::string Finder::find(uint32_t num_in) {
     clump_mass_threshold = p.min_trusted_mass;
     peak_density_threshold = 3 * density_threshold;
 
+    // PLAN_ORACLE_TRACE=1 prints the wall time of each phase to stderr
+    const bool trace_on = std::getenv("PLAN_ORACLE_TRACE") != nullptr;
+    auto t_last = std::chrono::steady_clock::now();
+    auto phase_mark = [&](const char *what) {
+        if (!trace_on) return;
+        auto t = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "[oracle] %-16s %9.1f ms\n", what, std::chrono::duration<double, std::milli>(t - t_last).count());
+        t_last = t;
+    };
     // 1. densities, src/tree.hpp:3667-3689
 #pragma omp parallel num_threads(threads)
     {
@@ -894,6 +904,7 @@ std::string Finder::find(uint32_t num_in) {
             tree.pts[i].new_density = density_kernel(h, (uint32_t)i, p.knn);
         }
     }
+    phase_mark("density");
     // 2. densest neighbour, src/tree.hpp:3711-3760
     densest.assign(T, 0);
 #pragma omp parallel num_threads(threads)
@@ -913,6 +924,7 @@ std::string Finder::find(uint32_t num_in) {
             }
         }
     }
+    phase_mark("densest");
     // 3. HOP chains, src/tree.hpp:3766-3809
     std::vector<char> open(T, 1);
     peak_of.assign(T, 0);
@@ -951,6 +963,7 @@ std::string Finder::find(uint32_t num_in) {
     num_planetesimals = (uint32_t)clumps.size();
     stats.naive_peaks = num_planetesimals;
 
+    phase_mark("hop");
     // 4. merge sweeps, src/tree.hpp:3863-4152
     Tree ct;
     for (int sweep_kind = 0; sweep_kind < 2; ++sweep_kind) {
@@ -1042,6 +1055,7 @@ std::string Finder::find(uint32_t num_in) {
             std::fprintf(stderr, "Real peak index replacing failed. \n");
         }
     }
+    phase_mark("merges+rekey");
     // 5. unbind and rebind, src/tree.hpp:4189-4208
     for (auto &it : clumps) {
         remove_unbound(it.second);
@@ -1056,6 +1070,7 @@ std::string Finder::find(uint32_t num_in) {
             hill(it.second);
         } while (it.second.indices.size() > before);
     }
+    phase_mark("unbind+rebind");
     // 6. prune, src/tree.hpp:4213-4224
     remove_small_and_low();
     for (auto &it : clumps)
@@ -1091,6 +1106,7 @@ std::string Finder::find(uint32_t num_in) {
     num_planetesimals = (uint32_t)clumps.size();
     std::ostringstream out;
     out << "Finish clump finding for t = " << time << ", ";
+    phase_mark("prune+rip+ghost");
     // 10. angular momentum and ranking, src/tree.hpp:4273-4326
     for (auto &it : clumps) angular_momentum(it.second);
     if (num_planetesimals > 0) {

@@ -203,7 +203,17 @@ int plan_stage_copy(plan_ctx *h, int which, void *dst, size_t bytes) {
     case PLAN_ARR_ORIG_ID: return copy(t.orig, n * 4);
     case PLAN_ARR_SINK_COUNT: return copy(t.sink_n, n * 4);
     case PLAN_ARR_DENSEST: return copy(c.densest, n * 4);
-    case PLAN_ARR_PEAK: return copy(c.peak, n * 4);
+    case PLAN_ARR_PEAK: {  // points below the density threshold belong to no group (src/tree.hpp:3775-3779)
+        if (bytes < n * 4) return kErrArgument;
+        std::vector<uint32_t> pk(n);
+        std::vector<double> dn(n);
+        PLAN_CUDA(cudaMemcpy(pk.data(), c.peak, n * 4, cudaMemcpyDeviceToHost));
+        PLAN_CUDA(cudaMemcpy(dn.data(), t.dens, n * 8, cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < n; ++i)
+            if (dn[i] < c.fs.density_threshold) pk[i] = (uint32_t)n;
+        std::memcpy(dst, pk.data(), n * 4);
+        return kOk;
+    }
     case PLAN_ARR_KEYS: {
         if (bytes < n * 12) return kErrArgument;
         std::vector<uint32_t> a(n), b(n), d(n);

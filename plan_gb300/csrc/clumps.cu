@@ -32,6 +32,7 @@
 #include "hop.h"
 #include "pipeline.h"
 #include "sort.h"
+#include "ordered_sum.cuh"
 #include "tree_walk.cuh"
 
 namespace plan {
@@ -40,6 +41,8 @@ namespace {
 
 constexpr uint32_t kNone = 0xffffffffu;
 constexpr int kSmallSort = 2048;
+constexpr uint32_t kBigKinematics = 4096;  // larger clumps sum with warp_ordered_sum
+constexpr int kKinTile = 512;
 
 struct CP {
     double G, shear, Omega;
@@ -82,6 +85,18 @@ __device__ __forceinline__ double norm2_3(double x, double y, double z) {
     return s;
 }
 
+// bump allocation that leaves the pool untouched when it does not fit
+__device__ uint32_t pool_try_alloc(const Pool &P, uint32_t n) {
+    uint32_t cur = *(volatile uint32_t *)P.top;
+    for (int it = 0; it < (1 << 22); ++it) {  // every failed exchange is another block's success
+        if ((uint64_t)cur + n > P.cap) return 0xffffffffu;
+        const uint32_t prev = atomicCAS(P.top, cur, cur + n);
+        if (prev == cur) return cur;
+        cur = prev;
+    }
+    return 0xffffffffu;
+}
+
 __device__ uint32_t pool_alloc(const Pool &P, uint32_t n, unsigned *err) {
     uint32_t o = atomicAdd(P.top, n);
     if (o + n > P.cap || o + n < o) {
@@ -122,6 +137,7 @@ __global__ void __launch_bounds__(128) k_kinematics(const uint32_t *list, uint32
     if (t >= n) return;
     const uint32_t s = list[t];
     const uint32_t o = ct.moff[s], m = ct.mn[s];
+    if (m > kBigKinematics) return;  // k_kinematics_big
     double acc = 0;  // lane c < 7 holds sum c: M, m*x, m*y, m*z, m*vx, m*vy, m*vz
     for (uint32_t base = 0; base < m; base += 32) {
         const uint32_t k = base + lane;
@@ -149,6 +165,45 @@ __global__ void __launch_bounds__(128) k_kinematics(const uint32_t *list, uint32
         ct.M[s] = M;
         ct.com[s] = make_double4_32a(cx / M, cy / M, cz / M, 0);
         ct.vcom[s] = make_double4_32a(vx / M, vy / M, vz / M, 0);
+        if (with_hill) ct.hill[s] = cr_pow_third(M * G / 3. / Omega / Omega);  // src/tree.hpp:4715-4717
+    }
+}
+
+// The same sums for clumps of more than kBigKinematics members: the block stages the terms
+// of kKinTile members in shared memory and warp c runs sum c with warp_ordered_sum.
+__global__ void __launch_bounds__(256) k_kinematics_big(const uint32_t *list, CT ct, Pool P, const double4_32a *pos, const double4_32a *vel,
+                                                        int with_hill, double G, double Omega) {
+    __shared__ double term[7][kKinTile];
+    __shared__ double res[7];
+    const uint32_t s = list[blockIdx.x];
+    const uint32_t o = ct.moff[s], m = ct.mn[s];
+    if (m <= kBigKinematics) return;
+    const int w = threadIdx.x >> 5;
+    double acc = 0.0;
+    for (uint32_t base = 0; base < m; base += kKinTile) {
+        const uint32_t cnt = min((uint32_t)kKinTile, m - base);
+        for (uint32_t i = threadIdx.x; i < cnt; i += blockDim.x) {
+            const uint32_t id = P.idx[o + base + i];
+            const double4_32a p = pos[id], v = vel[id];
+            term[0][i] = p.w;
+            term[1][i] = p.x * p.w;
+            term[2][i] = p.y * p.w;
+            term[3][i] = p.z * p.w;
+            term[4][i] = v.x * p.w;
+            term[5][i] = v.y * p.w;
+            term[6][i] = v.z * p.w;
+        }
+        __syncthreads();
+        if (w < 7) acc = warp_ordered_sum(term[w], cnt, acc);
+        __syncthreads();
+    }
+    if (w < 7 && (threadIdx.x & 31) == 0) res[w] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const double M = res[0];
+        ct.M[s] = M;
+        ct.com[s] = make_double4_32a(res[1] / M, res[2] / M, res[3] / M, 0);
+        ct.vcom[s] = make_double4_32a(res[4] / M, res[5] / M, res[6] / M, 0);
         if (with_hill) ct.hill[s] = cr_pow_third(M * G / 3. / Omega / Omega);  // src/tree.hpp:4715-4717
     }
 }
@@ -660,6 +715,8 @@ __global__ void __launch_bounds__(256) k_unbind(const uint32_t *list, CT ct, Poo
 // frontier entries, once to count and once to write the candidates at scanned offsets.
 constexpr int kFront = 2048;
 constexpr int kRebindThreads = 256;
+constexpr int kTile = 256;  // candidates staged per step of the acceptance: 64 B + 5 B each
+static_assert(kTile * (64 + 4 + 1) <= kFront * (3 * 4 + 2), "the candidate tile must fit in the frontier space");
 
 __global__ void k_elig_flags(uint32_t Tu, const uint8_t *in_clump, const double *dens, double thr, uint32_t *flag) {
     uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -743,6 +800,31 @@ __device__ void ball_walk_below(const KTree &t, const uint32_t *epos, uint32_t f
     atomicOr(err, (unsigned)kDevErrLoopLimit);
 }
 
+// IsGravitationallyBound for a candidate against the clump state, as the rebinding loop
+// evaluates it (src/tree.hpp:4686-4694): e = 0.5/(M+m) |v_com - shear - v|^2 - G/|r_com - r|,
+// bound when e < 0. The differences are formed in FP64 exactly as there; the rest runs in
+// FP32, where each of the two terms carries a relative error below 2^-20 (at most ten
+// roundings of 2^-24 on values far from the FP32 range limits). When the FP32 result is
+// farther than 2^-18 (|A| + |B|) from zero its sign is the sign of the FP64 expression;
+// otherwise the FP64 expression decides.
+__device__ __forceinline__ bool bound_after_adding(const double4_32a p, const double4_32a v, double sM, double x, double y, double z,
+                                                   double vx, double vy, double vz, const CP &cp) {
+    const double M = sM + p.w;
+    const double dx = x - p.x;
+    const double ex = (vx - 0.0 * dx) - v.x, ey = (vy - cp.shear * dx) - v.y, ez = (vz - 0.0 * dx) - v.z;
+    const double ry = y - p.y, rz = z - p.z;
+    const float fx = (float)ex, fy = (float)ey, fz = (float)ez, gx = (float)dx, gy = (float)ry, gz = (float)rz;
+    const float K = fx * fx + fy * fy + fz * fz, D2 = gx * gx + gy * gy + gz * gz;
+    if (K > 1e-30f && D2 > 1e-30f && K < 1e30f && D2 < 1e30f && M > 1e-30 && M < 1e30) {
+        const float A = 0.5f / (float)M * K, B = (float)cp.G / sqrtf(D2);
+        const float e = A - B, margin = (fabsf(A) + fabsf(B)) * 3.814697265625e-06f;  // 2^-18
+        if (e > margin) return false;
+        if (e < -margin) return true;
+    }
+    const double e = +0.5 / M * norm2_3(ex, ey, ez) - cp.G / norm3(dx, ry, rz);
+    return e < 0;
+}
+
 // Deferral records of a clump: the key ranks of the earlier clumps whose particles it
 // skipped (at most kDeferSlots distinct ranks; beyond that only the largest is known and
 // the host falls back to it).
@@ -775,11 +857,14 @@ __global__ void __launch_bounds__(kRebindThreads) k_rebind_round(const uint32_t 
                                                                  const uint32_t *rank_of, const uint32_t *slot_of_rank, uint8_t *invalid,
                                                                  uint32_t *dmax, uint32_t *dset, uint8_t *dover, int seq_mode, CP cp,
                                                                  uint8_t *grew, uint32_t *mn_out,
-                                                                 unsigned *err) {
+                                                                 unsigned *err, unsigned long long *prof, const double4_32a *com0,
+                                                                 unsigned long long *reach) {
     __shared__ double sM, scx, scy, scz, svx, svy, svz, c0x, c0y, c0z, rad;
-    __shared__ uint32_t s_first, s_noff, s_nacc, s_nf, s_expand;
-    __shared__ uint32_t front[kFront], front2[kFront], fcnt[kFront];
-    __shared__ uint8_t fcls[kFront], fcls2[kFront];
+    __shared__ uint32_t s_noff, s_nacc, s_nf, s_expand, s_at;
+    // the frontier arrays (steps 1-2) and the candidate tiles (step 3) share this space
+    __shared__ __align__(16) unsigned char sbuf[kFront * (3 * 4 + 2)];
+    uint32_t *front = reinterpret_cast<uint32_t *>(sbuf), *front2 = front + kFront, *fcnt = front2 + kFront;
+    uint8_t *fcls = reinterpret_cast<uint8_t *>(fcnt + kFront), *fcls2 = fcls + kFront;
     __shared__ uint32_t warp_tot[kRebindThreads / 32];
     const uint32_t slot = list[blockIdx.x];
     const uint32_t myrank = seq_mode ? 0u : rank_of[slot];
@@ -798,6 +883,13 @@ __global__ void __launch_bounds__(kRebindThreads) k_rebind_round(const uint32_t 
     }
     __syncthreads();
     const double cx = c0x, cy = c0y, cz = c0z, r = rad, rr = r * r;
+    const unsigned long long t_start = prof ? clock64() : 0;
+    if (threadIdx.x == 0) {  // how far this clump's balls reach from its centre before rebinding
+        const double4_32a c0 = com0[slot];
+        const double dx = cx - c0.x, dy = cy - c0.y, dz = cz - c0.z;
+        const double d = sqrt(dx * dx + dy * dy + dz * dz) + r;
+        if (d >= 0) atomicMax(&reach[slot], (unsigned long long)__double_as_longlong(d));
+    }
     // 1) breadth-first frontier (classes 1..4; 0 = not yet classified)
     for (int level = 0; level < 40; ++level) {
         const uint32_t nf = s_nf;
@@ -852,6 +944,7 @@ __global__ void __launch_bounds__(kRebindThreads) k_rebind_round(const uint32_t 
         fcls[i] = front[i] < t.nodes ? (uint8_t)ball_class(t, epos, front[i], cx, cy, cz, r, eb, ee) : (uint8_t)3;
     }
     __syncthreads();
+    const unsigned long long t_front = prof ? clock64() : 0;
     // 2) count the candidates below each frontier entry, then scan to offsets
     for (uint32_t i = threadIdx.x; i < nf; i += blockDim.x) {
         const uint32_t node = front[i];
@@ -873,11 +966,18 @@ __global__ void __launch_bounds__(kRebindThreads) k_rebind_round(const uint32_t 
     }
     __syncthreads();
     const uint32_t nel = block_scan_excl(fcnt, nf, warp_tot);
-    // segment: the members, the candidates in walk order, then the accepted ones (at most
-    // one per candidate)
-    if (threadIdx.x == 0) s_noff = pool_alloc(P, ct.mn[slot] + 2 * nel, err);
+    // segment: the members, then the candidates in walk order; the accepted ones overwrite
+    // the candidates already consumed, so the segment ends as members + accepted
+    if (threadIdx.x == 0) s_noff = pool_try_alloc(P, ct.mn[slot] + nel);
     __syncthreads();
-    if (s_noff == kNone) return;
+    if (s_noff == kNone) {  // the pool is full: the host compacts it and repeats this call
+        if (threadIdx.x == 0) {
+            grew[blockIdx.x] = 2;
+            mn_out[blockIdx.x] = ct.mn[slot];
+        }
+        return;
+    }
+    const unsigned long long t_count = prof ? clock64() : 0;
     const uint32_t m0 = ct.mn[slot], o = ct.moff[slot], no = s_noff;
     for (uint32_t k = threadIdx.x; k < m0; k += blockDim.x) P.idx[no + k] = P.idx[o + k];
     uint32_t *elig = P.idx + no + m0;  // candidates in walk order
@@ -898,63 +998,116 @@ __global__ void __launch_bounds__(kRebindThreads) k_rebind_round(const uint32_t 
         }
     }
     __syncthreads();
-    // 3) the reference's sequential acceptance over the candidates, a chunk at a time
-    uint32_t *acc = elig + nel;  // accepted, in acceptance order
-    uint32_t at = 0;
-    while (at < nel) {
-        if (threadIdx.x == 0) s_first = kNone;
-        __syncthreads();
-        uint32_t k = at + threadIdx.x;
-        bool bound = false;
-        if (k < nel) {
-            const uint32_t q2 = elig[k];
+    // 3) the reference's sequential acceptance over the candidates (src/tree.hpp:4686-4706).
+    // The block stages kTile candidates at a time in shared memory (positions, velocities,
+    // taken flags read now); warp 0 then walks them: the lanes test 32 candidates against
+    // the current state, the first bound one is taken and every lane applies the same FP64
+    // update to its copy of the state.
+    const unsigned long long t_fill = prof ? clock64() : 0;
+    uint32_t *acc = elig;  // accepted, in acceptance order, over the consumed candidates
+    __shared__ uint32_t s_iters;
+    double4_32a *tpos = reinterpret_cast<double4_32a *>(sbuf), *tvel = tpos + kTile;
+    uint32_t *tq = reinterpret_cast<uint32_t *>(tvel + kTile);
+    uint8_t *ttaken = reinterpret_cast<uint8_t *>(tq + kTile);
+    double M_ = 0, x_ = 0, y_ = 0, z_ = 0, vx_ = 0, vy_ = 0, vz_ = 0;  // warp 0's copy of the state
+    uint32_t nacc_ = 0, iters = 0;
+    if (threadIdx.x < 32) {
+        M_ = sM; x_ = scx; y_ = scy; z_ = scz; vx_ = svx; vy_ = svy; vz_ = svz;
+    }
+    if (threadIdx.x == 0) s_at = 0;
+    for (uint32_t base = 0; base < nel; base += kTile) {
+        const uint32_t tend = min(nel, base + (uint32_t)kTile);
+        for (uint32_t i = threadIdx.x; base + i < tend; i += blockDim.x) {
+            const uint32_t q2 = elig[base + i];
             bool taken = seq_mode && in_clump[q2] != 0;
             if (!taken && !seq_mode) {
-                uint32_t ow = owner[q2];
+                const uint32_t ow = __ldcg(&owner[q2]);
                 taken = ow != kNone && ow <= myrank;
                 if (ow != kNone && ow < myrank) defer_add(dset, dover, dmax, slot, ow);
             }
-            if (!taken) {
-                const double4_32a p = pos[q2], v = vel[q2];
-                double M = sM + p.w;
-                double dx = scx - p.x;
-                double ex = (svx - 0.0 * dx) - v.x, ey = (svy - cp.shear * dx) - v.y, ez = (svz - 0.0 * dx) - v.z;
-                double e = +0.5 / M * norm2_3(ex, ey, ez) - cp.G / norm3(scx - p.x, scy - p.y, scz - p.z);
-                bound = e < 0;
-            }
-        }
-        if (bound) atomicMin(&s_first, threadIdx.x);
-        __syncthreads();
-        const uint32_t f = s_first;
-        if (f == kNone) {
-            at += blockDim.x;
-            continue;
-        }
-        if (threadIdx.x == 0) {  // take it and update the state (src/tree.hpp:4696-4701)
-            const uint32_t q2 = elig[at + f];
-            const double4_32a p = pos[q2], v = vel[q2];
-            double M = sM + p.w;
-            scx = (scx * M + p.w * p.x) / M; scy = (scy * M + p.w * p.y) / M; scz = (scz * M + p.w * p.z) / M;
-            svx = (M * svx + p.w * v.x) / M; svy = (M * svy + p.w * v.y) / M; svz = (M * svz + p.w * v.z) / M;
-            sM = M;
-            if (seq_mode) {
-                in_clump[q2] = 1;
-            } else {
-                uint32_t old = atomicMin(&owner[q2], myrank);
-                if (old != kNone && old > myrank) invalid[slot_of_rank[old]] = 1;  // taken from a later clump
-                if (old != kNone && old < myrank) invalid[slot] = 1;               // an earlier clump got it first
-            }
-            acc[s_nacc] = q2;
-            s_nacc = s_nacc + 1;
+            tq[i] = q2;
+            ttaken[i] = taken ? 1 : 0;
+            tpos[i] = pos[q2];
+            tvel[i] = vel[q2];
         }
         __syncthreads();
-        at += f + 1;
+        if (threadIdx.x < 32) {
+            const int lane = threadIdx.x;
+            uint32_t at = s_at;
+            while (at < tend) {
+                ++iters;
+                const uint32_t k = at + lane;
+                bool bound = false;
+                if (k < tend && !ttaken[k - base]) bound = bound_after_adding(tpos[k - base], tvel[k - base], M_, x_, y_, z_, vx_, vy_, vz_, cp);
+                const unsigned b = __ballot_sync(0xffffffffu, bound);
+                if (!b) {
+                    at = min(at + 32, tend);
+                    continue;
+                }
+                const int f = __ffs(b) - 1;
+                const uint32_t j = at + f - base;
+                // src/tree.hpp:4696-4701 (the new mass multiplies the old centre); lane c < 6
+                // updates component c, then every lane takes all six
+                {
+                    // one division per lane, no divergence: component c is (s_c * M + m * q_c) / M
+                    // (M * s equals s * M bit for bit)
+                    const double4_32a p = tpos[j], v = tvel[j];
+                    const double M = M_ + p.w;
+                    const int c = lane < 6 ? lane : 0;
+                    const double sc = c == 0 ? x_ : c == 1 ? y_ : c == 2 ? z_ : c == 3 ? vx_ : c == 4 ? vy_ : vz_;
+                    const double qc = c == 0 ? p.x : c == 1 ? p.y : c == 2 ? p.z : c == 3 ? v.x : c == 4 ? v.y : v.z;
+                    const double r = (sc * M + p.w * qc) / M;
+                    x_ = __shfl_sync(0xffffffffu, r, 0);
+                    y_ = __shfl_sync(0xffffffffu, r, 1);
+                    z_ = __shfl_sync(0xffffffffu, r, 2);
+                    vx_ = __shfl_sync(0xffffffffu, r, 3);
+                    vy_ = __shfl_sync(0xffffffffu, r, 4);
+                    vz_ = __shfl_sync(0xffffffffu, r, 5);
+                    M_ = M;
+                }
+                if (lane == 0) {
+                    const uint32_t q2 = tq[j];
+                    if (seq_mode) {
+                        in_clump[q2] = 1;
+                    } else {
+                        const uint32_t old = atomicMin(&owner[q2], myrank);
+                        if (old != kNone && old > myrank) {  // taken from a later clump: it depends on this one
+                            invalid[slot_of_rank[old]] = 1;
+                            defer_add(dset, dover, dmax, slot_of_rank[old], myrank);
+                        }
+                        if (old != kNone && old < myrank) {  // an earlier clump got it first
+                            invalid[slot] = 1;
+                            defer_add(dset, dover, dmax, slot, old);
+                        }
+                    }
+                    acc[nacc_] = q2;
+                }
+                ++nacc_;
+                at += f + 1;
+            }
+            if (lane == 0) s_at = at;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        sM = M_; scx = x_; scy = y_; scz = z_; svx = vx_; svy = vy_; svz = vz_;
+        s_nacc = nacc_;
+        s_iters = iters;
     }
     __syncthreads();
-    const uint32_t nacc = s_nacc;
-    // members followed by the accepted ones (indices order of the reference)
-    for (uint32_t k = threadIdx.x; k < nacc; k += blockDim.x) P.idx[no + m0 + k] = acc[k];
-    __syncthreads();
+    const uint32_t nacc = s_nacc;  // members followed by the accepted ones (indices order of the reference)
+    if (threadIdx.x == 0 && prof) {
+        unsigned long long *q = prof + 8 * (size_t)blockIdx.x;
+        const unsigned long long t_end = clock64();
+        q[0] = t_front - t_start;
+        q[1] = t_count - t_front;
+        q[2] = t_fill - t_count;
+        q[3] = t_end - t_fill;
+        q[4] = nf;
+        q[5] = nel;
+        q[6] = nacc;
+        q[7] = ((unsigned long long)iters << 32) | m0;
+    }
     if (threadIdx.x == 0) {
         grew[blockIdx.x] = nacc ? 1 : 0;
         mn_out[blockIdx.x] = m0 + nacc;
@@ -1198,7 +1351,8 @@ struct Stage {
         if (rc) return rc;
         k_kinematics<<<(unsigned)((list.size() + 3) / 4), 128, 0, s>>>(d_list, (uint32_t)list.size(), ct, P, tr.pos, tr.vel, with_hill ? 1 : 0,
                                                                         cp.G, cp.Omega);
-        c.launches++;
+        k_kinematics_big<<<(unsigned)list.size(), 256, 0, s>>>(d_list, ct, P, tr.pos, tr.vel, with_hill ? 1 : 0, cp.G, cp.Omega);
+        c.launches += 2;
         PLAN_CUDA(cudaGetLastError());
         return kOk;
     }
@@ -1345,7 +1499,7 @@ struct Trace {
         on = e && *e && *e != '0';
         t0 = last = wall_ms();
     }
-    void mark(const char *what, long long a = -1, long long b = -1, long long c = -1) {
+    void mark(const char *what, long long a = -1, long long b = -1, long long c = -1, long long d = -1) {
         if (!on) return;
         cudaStreamSynchronize(s);
         double t = wall_ms();
@@ -1353,6 +1507,7 @@ struct Trace {
         if (a >= 0) std::fprintf(stderr, " %lld", a);
         if (b >= 0) std::fprintf(stderr, " %lld", b);
         if (c >= 0) std::fprintf(stderr, " %lld", c);
+        if (d >= 0) std::fprintf(stderr, " %lld", d);
         std::fprintf(stderr, "\n");
         last = t;
     }
@@ -1751,6 +1906,8 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
         uint8_t *dover = A.get<uint8_t>(nb);
         uint8_t *d_grew = A.get<uint8_t>(nb), *invalid = A.get<uint8_t>(nb), *rerun_rank = A.get<uint8_t>(nb);
         uint32_t *d_mnout = A.get<uint32_t>(nb);
+        unsigned long long *d_prof = trace.on ? A.get<unsigned long long>(8 * nb) : nullptr;
+        unsigned long long *reach = A.get<unsigned long long>(nb);
         if (A.failed) return kErrOutOfMemory;
         const uint32_t nlive = (uint32_t)live.size();
         // save the state (the member pool is packed first, then copied aside)
@@ -1786,11 +1943,33 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
         PLAN_CUDA(cudaMemsetAsync(dmax, 0, nb * 4, s));
         PLAN_CUDA(cudaMemsetAsync(dset, 0xff, nb * kDeferSlots * 4, s));
         PLAN_CUDA(cudaMemsetAsync(dover, 0, nb, s));
+        PLAN_CUDA(cudaMemsetAsync(reach, 0, nb * 8, s));
         KTree kt = ktree_of(tr);
         uint64_t rounds = 0, passes = 0, reruns = 0;
-        auto run_rounds = [&](std::vector<uint32_t> active, int seq_mode) -> int {
-            for (int round = 0; !active.empty(); ++round) {
+        // Rounds until no clump grows. Clumps in `waiting` start once every clump listed as
+        // their blocker has finished (reruns in key order where their balls may meet).
+        std::vector<uint8_t> finished(C, 0);
+        auto run_rounds = [&](std::vector<uint32_t> active, int seq_mode, std::vector<uint32_t> waiting,
+                              const std::vector<std::vector<uint32_t>> &blockers) -> int {
+            for (uint32_t sl : active) finished[sl] = 0;
+            for (uint32_t sl : waiting) finished[sl] = 0;
+            auto admit = [&](std::vector<uint32_t> &to) {
+                std::vector<uint32_t> keep;
+                for (uint32_t w : waiting) {
+                    bool ready = true;
+                    for (uint32_t b : blockers[w]) ready = ready && finished[b];
+                    if (ready) to.push_back(w);
+                    else keep.push_back(w);
+                }
+                waiting.swap(keep);
+            };
+            admit(active);
+            for (int round = 0; !active.empty() || !waiting.empty(); ++round) {
                 if (round > 200000) return kErrDeviceLimit;
+                if (active.empty()) {  // cannot happen with blockers of lower rank; start the first waiting clump
+                    active.push_back(waiting.front());
+                    waiting.erase(waiting.begin());
+                }
                 ++rounds;
                 int r = st.up_list(active, st.d_list);
                 if (r) return r;
@@ -1798,7 +1977,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                 k_rebind_round<<<(unsigned)active.size(), kRebindThreads, 0, s>>>(st.d_list, ct, P, kt, tr.vel, E, epos, in_clump, owner,
                                                                                   rank_of, slot_of_rank, invalid, dmax, dset, dover, seq_mode,
                                                                                   st.cp, d_grew,
-                                                                                  d_mnout, c.d_err);
+                                                                                  d_mnout, c.d_err, trace.on ? d_prof : nullptr, bc, reach);
                 c.launches++;
                 PLAN_CUDA(cudaGetLastError());
                 std::vector<uint8_t> g;
@@ -1806,33 +1985,108 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                 r = st.down(g, d_grew, active.size());
                 if (!r) r = st.down(mo, d_mnout, active.size());
                 if (r) return r;
+                // calls that found the member pool full (grew = 2) changed nothing: compact the
+                // pool and repeat them
+                for (int attempt = 0;; ++attempt) {
+                    std::vector<uint32_t> retry;
+                    std::vector<size_t> at_k;
+                    for (size_t k = 0; k < active.size(); ++k)
+                        if (g[k] == 2) { retry.push_back(active[k]); at_k.push_back(k); }
+                    if (retry.empty()) break;
+                    if (attempt > 0 && retry.size() == g.size()) return kErrOutOfMemory;
+                    r = st.maybe_compact(true);
+                    if (!r) r = st.up_list(retry, st.d_list);
+                    if (r) return r;
+                    k_rebind_round<<<(unsigned)retry.size(), kRebindThreads, 0, s>>>(st.d_list, ct, P, kt, tr.vel, E, epos, in_clump, owner,
+                                                                                     rank_of, slot_of_rank, invalid, dmax, dset, dover, seq_mode,
+                                                                                     st.cp, d_grew, d_mnout, c.d_err, nullptr, bc, reach);
+                    c.launches++;
+                    PLAN_CUDA(cudaGetLastError());
+                    std::vector<uint8_t> g2;
+                    std::vector<uint32_t> mo2;
+                    r = st.down(g2, d_grew, retry.size());
+                    if (!r) r = st.down(mo2, d_mnout, retry.size());
+                    if (r) return r;
+                    size_t still = 0;
+                    for (size_t q = 0; q < retry.size(); ++q) {
+                        g[at_k[q]] = g2[q];
+                        mo[at_k[q]] = mo2[q];
+                        still += g2[q] == 2;
+                    }
+                    if (still == retry.size()) return kErrOutOfMemory;  // no progress after compaction
+                    c.counters[22] += retry.size();
+                }
                 double t_b = wall_ms();
                 c.stage_ms[16] += t_b - t_a;
+                if (trace.on && (round % 25 == 0 || t_b - t_a > 20)) {
+                    std::vector<unsigned long long> pr;
+                    r = st.down(pr, d_prof, 8 * active.size());
+                    if (r) return r;
+                    unsigned long long mx[4] = {0, 0, 0, 0}, sum[4] = {0, 0, 0, 0};
+                    size_t worst = 0;
+                    unsigned long long worst_t = 0;
+                    for (size_t k = 0; k < active.size(); ++k) {
+                        unsigned long long tot = 0;
+                        for (int q = 0; q < 4; ++q) {
+                            mx[q] = std::max(mx[q], pr[8 * k + q]);
+                            sum[q] += pr[8 * k + q];
+                            tot += pr[8 * k + q];
+                        }
+                        if (tot > worst_t) { worst_t = tot; worst = k; }
+                    }
+                    const unsigned long long *w = &pr[8 * worst];
+                    std::fprintf(stderr,
+                                 "[plan]   rebind kernel %.1f ms, %zu blocks; max kcycles front %llu count %llu fill %llu accept %llu; "
+                                 "worst block: front %llu count %llu fill %llu accept %llu kcycles, nf %llu nel %llu nacc %llu iters %llu m0 %llu\n",
+                                 t_b - t_a, active.size(), mx[0] / 1000, mx[1] / 1000, mx[2] / 1000, mx[3] / 1000, w[0] / 1000, w[1] / 1000,
+                                 w[2] / 1000, w[3] / 1000, w[4], w[5], w[6], w[7] >> 32, w[7] & 0xffffffffull);
+                }
                 std::vector<uint32_t> grown, grown_mn;
                 for (size_t k = 0; k < active.size(); ++k)
-                    if (g[k]) { grown.push_back(active[k]); grown_mn.push_back(mo[k]); }
+                    if (g[k] == 1) { grown.push_back(active[k]); grown_mn.push_back(mo[k]); }
                 // SortParticles when the clump grew, then CalculateHillRadius (unchanged mass
                 // gives an unchanged radius for the others)
                 r = st.sort_particles(grown, false, true, &grown_mn);
                 if (!r) r = st.sync();
                 double t_c = wall_ms();
                 c.stage_ms[17] += t_c - t_b;
+                if (trace.on && (round % 25 == 0 || t_c - t_b > 20))
+                    std::fprintf(stderr, "[plan]   sort particles %.1f ms for %zu grown\n", t_c - t_b, grown.size());
                 if (!r) r = st.maybe_compact();
                 if (r) return r;
                 c.stage_ms[18] += wall_ms() - t_c;
                 uint64_t mx = 0;
                 for (uint32_t v : grown_mn) mx = std::max<uint64_t>(mx, v);
                 c.counters[16] = std::max<uint64_t>(c.counters[16], mx);
-                if (round % 25 == 0) trace.mark("rebinding round (round, grown, largest)", round, grown.size(), mx);
+                if (round % 25 == 0) trace.mark("rebinding round (round, grown, largest, waiting)", round, grown.size(), mx, waiting.size());
+                for (size_t k = 0; k < active.size(); ++k)
+                    if (g[k] != 1) finished[active[k]] = 1;
+                admit(grown);
                 active.swap(grown);
             }
             return kOk;
         };
+        const std::vector<std::vector<uint32_t>> no_blockers(C);
+        // reruns either start together (speculatively, as the first pass) or wait for the
+        // reruns they met in the previous pass (PLAN_RERUN_SCHEDULE=1)
+        const char *sched_env = std::getenv("PLAN_RERUN_SCHEDULE");
+        const bool schedule_reruns = sched_env && *sched_env == '1';
+        std::vector<std::vector<uint32_t>> blockers(C);
         std::vector<uint32_t> active = live;
         for (uint32_t pass = 0; !active.empty(); ++pass) {
             if (pass > nlive + 2) return kErrDeviceLimit;
             ++passes;
-            rc = run_rounds(active, 0);
+            std::vector<uint32_t> waiting;
+            if (pass > 0 && schedule_reruns) {  // the reruns start once the reruns they met in the last pass are done
+                std::vector<uint32_t> first;
+                for (uint32_t sa : active) {
+                    if (blockers[sa].empty()) first.push_back(sa);
+                    else waiting.push_back(sa);
+                }
+                trace.mark("rerun schedule (rerun, start now, wait)", active.size(), first.size(), waiting.size());
+                active.swap(first);
+            }
+            rc = run_rounds(active, 0, waiting, (pass > 0 && schedule_reruns) ? blockers : no_blockers);
             if (rc) return rc;
             std::vector<uint8_t> inv, dov;
             std::vector<uint32_t> dm, ds;
@@ -1860,6 +2114,33 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                     }
                 }
                 if (again) { rerun.push_back(sl); rr[r] = 1; }
+            }
+            // blockers of each rerun clump: the rerun clumps of lower rank it met (skipped a
+            // particle of, lost one to, or had one taken by); when its record overflowed, every
+            // lower rerun clump whose balls came within reach
+            std::vector<unsigned long long> rb;
+            std::vector<double4_32a> c0;
+            rc = st.down(rb, reach, C);
+            if (!rc) rc = st.down(c0, bc, C);
+            if (rc) return rc;
+            for (size_t a = 0; a < rerun.size(); ++a) {
+                const uint32_t sa = rerun[a];
+                blockers[sa].clear();
+                if (!dov[sa]) {
+                    for (int j = 0; j < kDeferSlots; ++j) {
+                        const uint32_t d = ds[(size_t)sa * kDeferSlots + j];
+                        if (d != kNone && d < nlive && rr[d] && live[d] != sa) blockers[sa].push_back(live[d]);
+                    }
+                } else {
+                    const double ra = __builtin_bit_cast(double, rb[sa]);
+                    for (size_t b = 0; b < a; ++b) {  // rerun is in key order
+                        const uint32_t sb = rerun[b];
+                        const double r2 = __builtin_bit_cast(double, rb[sb]);
+                        const double dx = c0[sa].x - c0[sb].x, dy = c0[sa].y - c0[sb].y, dz = c0[sa].z - c0[sb].z;
+                        const double lim = 1.25 * (ra + r2) + 1e-12;
+                        if (dx * dx + dy * dy + dz * dz <= lim * lim) blockers[sa].push_back(sb);
+                    }
+                }
             }
             reruns += rerun.size();
             PLAN_CUDA(cudaMemcpyAsync(rerun_rank, rr.data(), nlive, cudaMemcpyHostToDevice, s));

@@ -161,3 +161,33 @@ def test_repeat_runs_identical(pg, case_dir):
         assert out[0] != out[1]
     finally:
         f.close()
+
+
+@pytest.mark.parametrize("n,seed", [(1 << 20, 2), (1 << 21, 4)])
+def test_large_snapshot_against_oracle(n, seed, pg, finder, tmp_path):
+    """Snapshots of 1M and 2M particles of the 16.7M workload's mixture: clumps of tens of
+    thousands of members take the large-clump paths (ordered sums over warps, the radix sort
+    of member distances, concurrent Hill rebinding with reruns). The catalogue must equal the
+    oracle's byte for byte, and densities and densest pointers bit for bit."""
+    import oracle
+
+    c = cases.Case(f"w2_{n}", 2, n, seed, 128)
+    m = cases.materialise(c, tmp_path / "in")
+    p = pg.params(m["param"])
+    snap = pg.Snapshot(m["lis"])
+    cat = finder.find_clumps(snap, p)
+    o = oracle.Oracle(m["lis"], m["param"], threads=os.cpu_count() or 1, pow_mode=1)
+    o.find()
+    f9 = o.points()[0]
+    np.testing.assert_array_equal(finder.stage(pg.PLAN_ARR_DENSITY), f9[:, 8])
+    np.testing.assert_array_equal(finder.stage(pg.PLAN_ARR_DENSEST), o.densest())
+    assert cat.summary().strip() == o.summary().strip()
+    (tmp_path / "g").mkdir()
+    (tmp_path / "o").mkdir()
+    cat.write_peaks(str(tmp_path / "g" / "res.txt"))
+    o.write_outputs(str(tmp_path / "o" / "res.txt"))
+    pg_file = cases.find_peaks_file(tmp_path / "g")
+    assert pg_file.read_bytes() == cases.find_peaks_file(tmp_path / "o").read_bytes()
+    assert len(cat) > 0
+    cat.close()
+    snap.close()
