@@ -34,6 +34,7 @@
 #include "sort.h"
 #include "ordered_sum.cuh"
 #include "tree_walk.cuh"
+#include "knn_f32.cuh"
 
 namespace plan {
 
@@ -213,7 +214,8 @@ __global__ void k_dist(const uint32_t *list, CT ct, Pool P, const double4_32a *p
     uint32_t s = list[blockIdx.x];
     const uint32_t o = ct.moff[s], m = ct.mn[s];
     double4_32a c = ct.com[s];
-    for (uint32_t k = threadIdx.x; k < m; k += blockDim.x) {
+    // gridDim.y blocks share a clump (large clumps spread their FP64 work over several SMs)
+    for (uint32_t k = blockIdx.y * blockDim.x + threadIdx.x; k < m; k += blockDim.x * gridDim.y) {
         double4_32a p = pos[P.idx[o + k]];
         P.dist[o + k] = norm3(p.x - c.x, p.y - c.y, p.z - c.z);
     }
@@ -715,8 +717,9 @@ __global__ void __launch_bounds__(256) k_unbind(const uint32_t *list, CT ct, Poo
 // frontier entries, once to count and once to write the candidates at scanned offsets.
 constexpr int kFront = 2048;
 constexpr int kRebindThreads = 256;
-constexpr int kTile = 256;  // candidates staged per step of the acceptance: 64 B + 5 B each
-static_assert(kTile * (64 + 4 + 1) <= kFront * (3 * 4 + 2), "the candidate tile must fit in the frontier space");
+constexpr int kCopyTasks = 512;  // queued copies of contained runs in the fill step
+constexpr int kTile = 192;  // candidates staged per step of the acceptance: 64 + 52 + 4 + 1 B each
+static_assert(kTile * (64 + 52 + 4 + 1) <= kFront * (3 * 4 + 2), "the candidate tile must fit in the frontier space");
 
 __global__ void k_elig_flags(uint32_t Tu, const uint8_t *in_clump, const double *dens, double thr, uint32_t *flag) {
     uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -759,21 +762,51 @@ __device__ uint32_t block_scan_excl(uint32_t *a, uint32_t n, uint32_t *warp_tot)
 
 // Node classes of the frontier: 1 contained (all candidates), 2 leaf reached but not
 // contained (candidates filtered by distance), 3 nothing, 4 descend into the children.
-__device__ __forceinline__ int ball_class(const KTree &t, const uint32_t *epos, uint32_t node, double cx, double cy, double cz, double r,
-                                          uint32_t &eb, uint32_t &ee) {
+// The ball of one SearchBound call: centre and radius in FP64, and as float hi/lo pairs for
+// the filtered tests (knn_f32.cuh: a decided FP32 test always agrees with the FP64 one).
+struct BallQ {
+    double cx, cy, cz, r, rr;
+    float4 qh, ql;
+    float rf, rr32;
+};
+
+__device__ __forceinline__ BallQ make_ball(double cx, double cy, double cz, double r) {
+    BallQ b;
+    b.cx = cx; b.cy = cy; b.cz = cz; b.r = r; b.rr = r * r;
+    const float hx = (float)cx, hy = (float)cy, hz = (float)cz;
+    b.qh = make_float4(hx, hy, hz, 0.f);
+    b.ql = make_float4((float)(cx - (double)hx), (float)(cy - (double)hy), (float)(cz - (double)hz), 0.f);
+    b.rf = (float)r;
+    b.rr32 = (float)b.rr;
+    return b;
+}
+
+// RecursiveBallSearch keeps a leaf point when its squared distance is <= r^2
+__device__ __forceinline__ bool in_ball(const KTree &t, const FTree &f, const BallQ &b, uint32_t p) {
+    const float v = f_dr2(b.qh, b.ql, f.phi[p], f.plo[p]);
+    if (f_hi(v) < b.rr32 * (1.f - kRel)) return true;
+    if (f_lo(v) > b.rr32 * (1.f + kRel)) return false;
+    return point_dr2(b.cx, b.cy, b.cz, t.pos[p]) <= b.rr;
+}
+
+__device__ __forceinline__ int ball_class(const KTree &t, const FTree &f, const uint32_t *epos, uint32_t node, const BallQ &b, uint32_t &eb,
+                                          uint32_t &ee) {
     eb = epos[t.nbeg[node]];
     ee = epos[t.nend[node]];
     if (eb == ee) return 3;
-    const double4_32a nc = t.ncf[node];
-    if (node_contained(nc, cx, cy, cz, r)) return 1;
-    if (node_intersects(nc, cx, cy, cz, r)) return t.nnd[node] == 0 ? 2 : 4;
+    const float4 nh = f.nhi[node], nl = f.nlo[node];
+    int cont = f_contained(nh, nl, b.qh, b.ql, b.rf);
+    if (cont < 0) cont = node_contained(t.ncf[node], b.cx, b.cy, b.cz, b.r) ? 1 : 0;
+    if (cont) return 1;
+    int inter = f_intersects(nh, nl, b.qh, b.ql, b.rf);
+    if (inter < 0) inter = node_intersects(t.ncf[node], b.cx, b.cy, b.cz, b.r) ? 1 : 0;
+    if (inter) return t.nnd[node] == 0 ? 2 : 4;
     return 3;
 }
 
 // the candidates below a class-4 node f, in point order
 template <class Emit>
-__device__ void ball_walk_below(const KTree &t, const uint32_t *epos, uint32_t f, double cx, double cy, double cz, double r, Emit emit,
-                                unsigned *err) {
+__device__ void ball_walk_below(const KTree &t, const FTree &ft, const uint32_t *epos, uint32_t f, const BallQ &b, Emit emit, unsigned *err) {
     uint32_t node = t.nfd[f];
     for (uint32_t guard = 0; guard < 4u * t.nodes + 8u; ++guard) {
         if (node >= t.nodes) {
@@ -781,7 +814,7 @@ __device__ void ball_walk_below(const KTree &t, const uint32_t *epos, uint32_t f
             return;
         }
         uint32_t eb, ee;
-        const int cls = ball_class(t, epos, node, cx, cy, cz, r, eb, ee);
+        const int cls = ball_class(t, ft, epos, node, b, eb, ee);
         if (cls == 1 || cls == 2) emit(eb, ee, cls == 2);
         if (cls == 4) {
             node = t.nfd[node];
@@ -802,27 +835,52 @@ __device__ void ball_walk_below(const KTree &t, const uint32_t *epos, uint32_t f
 
 // IsGravitationallyBound for a candidate against the clump state, as the rebinding loop
 // evaluates it (src/tree.hpp:4686-4694): e = 0.5/(M+m) |v_com - shear - v|^2 - G/|r_com - r|,
-// bound when e < 0. The differences are formed in FP64 exactly as there; the rest runs in
-// FP32, where each of the two terms carries a relative error below 2^-20 (at most ten
-// roundings of 2^-24 on values far from the FP32 range limits). When the FP32 result is
-// farther than 2^-18 (|A| + |B|) from zero its sign is the sign of the FP64 expression;
-// otherwise the FP64 expression decides.
-__device__ __forceinline__ bool bound_after_adding(const double4_32a p, const double4_32a v, double sM, double x, double y, double z,
-                                                   double vx, double vy, double vz, const CP &cp) {
+// bound when e < 0.
+// The same test in FP64 only, as the reference writes it.
+__device__ __forceinline__ bool bound_fp64(const double4_32a p, const double4_32a v, double sM, double x, double y, double z, double vx,
+                                          double vy, double vz, const CP &cp) {
     const double M = sM + p.w;
     const double dx = x - p.x;
     const double ex = (vx - 0.0 * dx) - v.x, ey = (vy - cp.shear * dx) - v.y, ez = (vz - 0.0 * dx) - v.z;
-    const double ry = y - p.y, rz = z - p.z;
-    const float fx = (float)ex, fy = (float)ey, fz = (float)ez, gx = (float)dx, gy = (float)ry, gz = (float)rz;
-    const float K = fx * fx + fy * fy + fz * fz, D2 = gx * gx + gy * gy + gz * gz;
-    if (K > 1e-30f && D2 > 1e-30f && K < 1e30f && D2 < 1e30f && M > 1e-30 && M < 1e30) {
-        const float A = 0.5f / (float)M * K, B = (float)cp.G / sqrtf(D2);
-        const float e = A - B, margin = (fabsf(A) + fabsf(B)) * 3.814697265625e-06f;  // 2^-18
-        if (e > margin) return false;
-        if (e < -margin) return true;
-    }
-    const double e = +0.5 / M * norm2_3(ex, ey, ez) - cp.G / norm3(dx, ry, rz);
+    const double e = +0.5 / M * norm2_3(ex, ey, ez) - cp.G / norm3(dx, y - p.y, z - p.z);
     return e < 0;
+}
+
+// A candidate as float hi/lo pairs (x = hi + lo to 2^-48): position, velocity, and its mass.
+struct CandF {
+    float ph[3], pl[3], vh[3], vl[3], w;
+};
+
+// The boundness test entirely in FP32 from hi/lo pairs of the state (sh, sl: x, y, z, vx,
+// vy, vz) and of the candidate: 1 bound, 0 not, -1 too close to call (then bound_fp64).
+// Differences of hi/lo pairs carry a relative error below 2^-23 (plus 2^-48 of the
+// coordinates from the splits); the y velocity term, a difference of two such values, carries
+// an absolute error below 2^-21 (|T1| + |T2|). With at most ten further FP32 roundings per
+// term, |A - A_exact| <= A 2^-20 + |ey| err_y / M and |B - B_exact| <= B 2^-20, inside the
+// margin below; the reference's own FP64 rounding is far smaller.
+__device__ __forceinline__ int bound_hilo(const CandF &c, float Mf, const float sh[6], const float sl[6], float G, float shear) {
+    const float dx = (sh[0] - c.ph[0]) + (sl[0] - c.pl[0]);
+    const float dy = (sh[1] - c.ph[1]) + (sl[1] - c.pl[1]);
+    const float dz = (sh[2] - c.ph[2]) + (sl[2] - c.pl[2]);
+    const float ex = (sh[3] - c.vh[0]) + (sl[3] - c.vl[0]);
+    const float t1 = (sh[4] - c.vh[1]) + (sl[4] - c.vl[1]), t2 = shear * dx;
+    const float ey = t1 - t2;
+    const float ez = (sh[5] - c.vh[2]) + (sl[5] - c.vl[2]);
+    const float K = ex * ex + ey * ey + ez * ez, D2 = dx * dx + dy * dy + dz * dz;
+    const float M = Mf + c.w;
+    if (!(K > 1e-30f && D2 > 1e-30f && K < 1e30f && D2 < 1e30f && M > 1e-30f && M < 1e30f)) return -1;
+    const float A = 0.5f / M * K, B = G / sqrtf(D2);
+    const float e = A - B;
+    const float margin = (fabsf(A) + fabsf(B)) * 3.814697265625e-06f                             // 2^-18
+                         + fabsf(ey) * (fabsf(t1) + fabsf(t2)) * 9.5367431640625e-07f / M;    // 2^-20 / M
+    if (e > margin) return 0;
+    if (e < -margin) return 1;
+    return -1;
+}
+
+__device__ __forceinline__ void split_f(double d, float &hi, float &lo) {
+    hi = (float)d;
+    lo = (float)(d - (double)hi);
 }
 
 // Deferral records of a clump: the key ranks of the earlier clumps whose particles it
@@ -858,9 +916,10 @@ __global__ void __launch_bounds__(kRebindThreads) k_rebind_round(const uint32_t 
                                                                  uint32_t *dmax, uint32_t *dset, uint8_t *dover, int seq_mode, CP cp,
                                                                  uint8_t *grew, uint32_t *mn_out,
                                                                  unsigned *err, unsigned long long *prof, const double4_32a *com0,
-                                                                 unsigned long long *reach) {
+                                                                 unsigned long long *reach, const uint32_t *tent, FTree ft) {
     __shared__ double sM, scx, scy, scz, svx, svy, svz, c0x, c0y, c0z, rad;
-    __shared__ uint32_t s_noff, s_nacc, s_nf, s_expand, s_at;
+    __shared__ uint32_t s_noff, s_nacc, s_nf, s_expand, s_at, s_next, s_ntask;
+    __shared__ uint32_t task_src[kCopyTasks], task_len[kCopyTasks], task_dst[kCopyTasks];
     // the frontier arrays (steps 1-2) and the candidate tiles (step 3) share this space
     __shared__ __align__(16) unsigned char sbuf[kFront * (3 * 4 + 2)];
     uint32_t *front = reinterpret_cast<uint32_t *>(sbuf), *front2 = front + kFront, *fcnt = front2 + kFront;
@@ -882,7 +941,8 @@ __global__ void __launch_bounds__(kRebindThreads) k_rebind_round(const uint32_t 
         s_nf = 1;
     }
     __syncthreads();
-    const double cx = c0x, cy = c0y, cz = c0z, r = rad, rr = r * r;
+    const double cx = c0x, cy = c0y, cz = c0z, r = rad;
+    const BallQ ball = make_ball(cx, cy, cz, r);
     const unsigned long long t_start = prof ? clock64() : 0;
     if (threadIdx.x == 0) {  // how far this clump's balls reach from its centre before rebinding
         const double4_32a c0 = com0[slot];
@@ -904,7 +964,7 @@ __global__ void __launch_bounds__(kRebindThreads) k_rebind_round(const uint32_t 
                     cls = 3;
                 } else {
                     uint32_t eb, ee;
-                    cls = ball_class(t, epos, node, cx, cy, cz, r, eb, ee);
+                    cls = ball_class(t, ft, epos, node, ball, eb, ee);
                 }
                 fcls[i] = (uint8_t)cls;
             }
@@ -941,12 +1001,15 @@ __global__ void __launch_bounds__(kRebindThreads) k_rebind_round(const uint32_t 
     for (uint32_t i = threadIdx.x; i < nf; i += blockDim.x) {  // entries left unclassified by the level cap
         if (fcls[i] != 0) continue;
         uint32_t eb, ee;
-        fcls[i] = front[i] < t.nodes ? (uint8_t)ball_class(t, epos, front[i], cx, cy, cz, r, eb, ee) : (uint8_t)3;
+        fcls[i] = front[i] < t.nodes ? (uint8_t)ball_class(t, ft, epos, front[i], ball, eb, ee) : (uint8_t)3;
     }
     __syncthreads();
     const unsigned long long t_front = prof ? clock64() : 0;
-    // 2) count the candidates below each frontier entry, then scan to offsets
-    for (uint32_t i = threadIdx.x; i < nf; i += blockDim.x) {
+    // 2) count the candidates below each frontier entry (entries handed out one at a time,
+    // the subtrees differ a lot in size), then scan to offsets
+    if (threadIdx.x == 0) s_next = 0;
+    __syncthreads();
+    for (uint32_t i = atomicAdd(&s_next, 1u); i < nf; i = atomicAdd(&s_next, 1u)) {
         const uint32_t node = front[i];
         const int cls = fcls[i];
         uint32_t cnt = 0;
@@ -954,13 +1017,13 @@ __global__ void __launch_bounds__(kRebindThreads) k_rebind_round(const uint32_t 
             if (!partial) {
                 cnt += ee - eb;
             } else {
-                for (uint32_t j = eb; j < ee; ++j) cnt += point_dr2(cx, cy, cz, pos[E[j]]) <= rr ? 1u : 0u;
+                for (uint32_t j = eb; j < ee; ++j) cnt += in_ball(t, ft, ball, E[j]) ? 1u : 0u;
             }
         };
         if (cls == 1 || cls == 2) {
             count(epos[t.nbeg[node]], epos[t.nend[node]], cls == 2);
         } else if (cls == 4) {
-            ball_walk_below(t, epos, node, cx, cy, cz, r, count, err);
+            ball_walk_below(t, ft, epos, node, ball, count, err);
         }
         fcnt[i] = cnt;
     }
@@ -981,21 +1044,43 @@ __global__ void __launch_bounds__(kRebindThreads) k_rebind_round(const uint32_t 
     const uint32_t m0 = ct.mn[slot], o = ct.moff[slot], no = s_noff;
     for (uint32_t k = threadIdx.x; k < m0; k += blockDim.x) P.idx[no + k] = P.idx[o + k];
     uint32_t *elig = P.idx + no + m0;  // candidates in walk order
-    for (uint32_t i = threadIdx.x; i < nf; i += blockDim.x) {
+    // long runs of a contained node are queued and copied by the whole block afterwards
+    if (threadIdx.x == 0) {
+        s_next = 0;
+        s_ntask = 0;
+    }
+    __syncthreads();
+    for (uint32_t i = atomicAdd(&s_next, 1u); i < nf; i = atomicAdd(&s_next, 1u)) {
         const uint32_t node = front[i];
         const int cls = fcls[i];
         uint32_t w = fcnt[i];
         auto fill = [&](uint32_t eb, uint32_t ee, bool partial) {
+            if (!partial && ee - eb > 64) {
+                const uint32_t slot_t = atomicAdd(&s_ntask, 1u);
+                if (slot_t < kCopyTasks) {
+                    task_src[slot_t] = eb;
+                    task_len[slot_t] = ee - eb;
+                    task_dst[slot_t] = w;
+                    w += ee - eb;
+                    return;
+                }
+            }
             for (uint32_t j = eb; j < ee; ++j) {
                 const uint32_t q = E[j];
-                if (!partial || point_dr2(cx, cy, cz, pos[q]) <= rr) elig[w++] = q;
+                if (!partial || in_ball(t, ft, ball, q)) elig[w++] = q;
             }
         };
         if (cls == 1 || cls == 2) {
             fill(epos[t.nbeg[node]], epos[t.nend[node]], cls == 2);
         } else if (cls == 4) {
-            ball_walk_below(t, epos, node, cx, cy, cz, r, fill, err);
+            ball_walk_below(t, ft, epos, node, ball, fill, err);
         }
+    }
+    __syncthreads();
+    const uint32_t ntask = min(s_ntask, (uint32_t)kCopyTasks);
+    for (uint32_t k = 0; k < ntask; ++k) {
+        const uint32_t src = task_src[k], len = task_len[k], dst = task_dst[k];
+        for (uint32_t j = threadIdx.x; j < len; j += blockDim.x) elig[dst + j] = E[src + j];
     }
     __syncthreads();
     // 3) the reference's sequential acceptance over the candidates (src/tree.hpp:4686-4706).
@@ -1007,12 +1092,18 @@ __global__ void __launch_bounds__(kRebindThreads) k_rebind_round(const uint32_t 
     uint32_t *acc = elig;  // accepted, in acceptance order, over the consumed candidates
     __shared__ uint32_t s_iters;
     double4_32a *tpos = reinterpret_cast<double4_32a *>(sbuf), *tvel = tpos + kTile;
-    uint32_t *tq = reinterpret_cast<uint32_t *>(tvel + kTile);
+    CandF *tf = reinterpret_cast<CandF *>(tvel + kTile);
+    uint32_t *tq = reinterpret_cast<uint32_t *>(tf + kTile);
     uint8_t *ttaken = reinterpret_cast<uint8_t *>(tq + kTile);
     double M_ = 0, x_ = 0, y_ = 0, z_ = 0, vx_ = 0, vy_ = 0, vz_ = 0;  // warp 0's copy of the state
+    float sh[6], sl[6], Mf = 0.f;                                      // and its float hi/lo pairs
+    const float G32 = (float)cp.G, shear32 = (float)cp.shear;
     uint32_t nacc_ = 0, iters = 0;
     if (threadIdx.x < 32) {
         M_ = sM; x_ = scx; y_ = scy; z_ = scz; vx_ = svx; vy_ = svy; vz_ = svz;
+        split_f(x_, sh[0], sl[0]); split_f(y_, sh[1], sl[1]); split_f(z_, sh[2], sl[2]);
+        split_f(vx_, sh[3], sl[3]); split_f(vy_, sh[4], sl[4]); split_f(vz_, sh[5], sl[5]);
+        Mf = (float)M_;
     }
     if (threadIdx.x == 0) s_at = 0;
     for (uint32_t base = 0; base < nel; base += kTile) {
@@ -1021,14 +1112,27 @@ __global__ void __launch_bounds__(kRebindThreads) k_rebind_round(const uint32_t 
             const uint32_t q2 = elig[base + i];
             bool taken = seq_mode && in_clump[q2] != 0;
             if (!taken && !seq_mode) {
-                const uint32_t ow = __ldcg(&owner[q2]);
-                taken = ow != kNone && ow <= myrank;
+                // held by this or an earlier clump, or predicted (from the last pass) to end
+                // up with an earlier clump that is being rerun
+                const uint32_t ow = __ldcg(&owner[q2]), tn = tent[q2];
+                taken = (ow != kNone && ow <= myrank) || (tn != kNone && tn < myrank);
                 if (ow != kNone && ow < myrank) defer_add(dset, dover, dmax, slot, ow);
+                else if (tn != kNone && tn < myrank) defer_add(dset, dover, dmax, slot, tn);
             }
             tq[i] = q2;
             ttaken[i] = taken ? 1 : 0;
-            tpos[i] = pos[q2];
-            tvel[i] = vel[q2];
+            const double4_32a pp = pos[q2], vv = vel[q2];
+            tpos[i] = pp;
+            tvel[i] = vv;
+            CandF cf;
+            split_f(pp.x, cf.ph[0], cf.pl[0]);
+            split_f(pp.y, cf.ph[1], cf.pl[1]);
+            split_f(pp.z, cf.ph[2], cf.pl[2]);
+            split_f(vv.x, cf.vh[0], cf.vl[0]);
+            split_f(vv.y, cf.vh[1], cf.vl[1]);
+            split_f(vv.z, cf.vh[2], cf.vl[2]);
+            cf.w = (float)pp.w;
+            tf[i] = cf;
         }
         __syncthreads();
         if (threadIdx.x < 32) {
@@ -1038,7 +1142,10 @@ __global__ void __launch_bounds__(kRebindThreads) k_rebind_round(const uint32_t 
                 ++iters;
                 const uint32_t k = at + lane;
                 bool bound = false;
-                if (k < tend && !ttaken[k - base]) bound = bound_after_adding(tpos[k - base], tvel[k - base], M_, x_, y_, z_, vx_, vy_, vz_, cp);
+                if (k < tend && !ttaken[k - base]) {
+                    const int r = bound_hilo(tf[k - base], Mf, sh, sl, G32, shear32);
+                    bound = r >= 0 ? r == 1 : bound_fp64(tpos[k - base], tvel[k - base], M_, x_, y_, z_, vx_, vy_, vz_, cp);
+                }
                 const unsigned b = __ballot_sync(0xffffffffu, bound);
                 if (!b) {
                     at = min(at + 32, tend);
@@ -1057,6 +1164,12 @@ __global__ void __launch_bounds__(kRebindThreads) k_rebind_round(const uint32_t 
                     const double sc = c == 0 ? x_ : c == 1 ? y_ : c == 2 ? z_ : c == 3 ? vx_ : c == 4 ? vy_ : vz_;
                     const double qc = c == 0 ? p.x : c == 1 ? p.y : c == 2 ? p.z : c == 3 ? v.x : c == 4 ? v.y : v.z;
                     const double r = (sc * M + p.w * qc) / M;
+                    float rh, rl;
+                    split_f(r, rh, rl);
+                    for (int q = 0; q < 6; ++q) {
+                        sh[q] = __shfl_sync(0xffffffffu, rh, q);
+                        sl[q] = __shfl_sync(0xffffffffu, rl, q);
+                    }
                     x_ = __shfl_sync(0xffffffffu, r, 0);
                     y_ = __shfl_sync(0xffffffffu, r, 1);
                     z_ = __shfl_sync(0xffffffffu, r, 2);
@@ -1064,21 +1177,16 @@ __global__ void __launch_bounds__(kRebindThreads) k_rebind_round(const uint32_t 
                     vy_ = __shfl_sync(0xffffffffu, r, 4);
                     vz_ = __shfl_sync(0xffffffffu, r, 5);
                     M_ = M;
+                    Mf = (float)M;
                 }
                 if (lane == 0) {
                     const uint32_t q2 = tq[j];
                     if (seq_mode) {
                         in_clump[q2] = 1;
                     } else {
-                        const uint32_t old = atomicMin(&owner[q2], myrank);
-                        if (old != kNone && old > myrank) {  // taken from a later clump: it depends on this one
-                            invalid[slot_of_rank[old]] = 1;
-                            defer_add(dset, dover, dmax, slot_of_rank[old], myrank);
-                        }
-                        if (old != kNone && old < myrank) {  // an earlier clump got it first
-                            invalid[slot] = 1;
-                            defer_add(dset, dover, dmax, slot, old);
-                        }
+                        // the lowest rank keeps the particle; who lost one is found after the
+                        // pass (k_rebind_verify), so the claim does not wait for the old value
+                        atomicMin(&owner[q2], myrank);
                     }
                     acc[nacc_] = q2;
                 }
@@ -1152,11 +1260,56 @@ __global__ void k_rebind_restore(const uint32_t *list, uint32_t n, CT ct, Pool P
     }
 }
 
-__global__ void k_rebind_release(uint32_t Tu, uint32_t *owner, const uint8_t *rerun_rank) {
+// After a pass: a clump whose accepted particles are not all still its own lost one to an
+// earlier clump (the claims keep the lowest rank); it is invalid and depends on that clump.
+__global__ void k_rebind_verify(const uint32_t *list, uint32_t n, CT ct, Pool P, const uint8_t *in_clump, const uint32_t *owner,
+                                const uint32_t *rank_of, uint8_t *invalid, uint32_t *dset, uint8_t *dover, uint32_t *dmax) {
+    if (blockIdx.x >= n) return;
+    const uint32_t s = list[blockIdx.x];
+    const uint32_t myrank = rank_of[s], o = ct.moff[s], m = ct.mn[s];
+    for (uint32_t k = threadIdx.x; k < m; k += blockDim.x) {
+        const uint32_t q = P.idx[o + k];
+        if (in_clump[q]) continue;  // a member before rebinding
+        const uint32_t w = owner[q];
+        if (w != myrank) {
+            invalid[s] = 1;
+            if (w != kNone && w < myrank) defer_add(dset, dover, dmax, s, w);
+        }
+    }
+}
+
+// Before a rerun pass: the particles of the clumps to be rerun become predictions (tent) of
+// who ends up with them; every other entry is a final holding.
+__global__ void k_rebind_tentative(uint32_t Tu, uint32_t *owner, uint32_t *tent, const uint8_t *rerun_rank) {
     uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= Tu) return;
-    uint32_t o = owner[q];
-    if (o != kNone && rerun_rank[o]) owner[q] = kNone;
+    const uint32_t o = owner[q];
+    if (o != kNone && rerun_rank[o]) {
+        tent[q] = o;
+        owner[q] = kNone;
+    } else {
+        tent[q] = kNone;
+    }
+}
+
+// order-independent hash of a clump's member set
+__global__ void k_member_hash(const uint32_t *list, uint32_t n, CT ct, Pool P, unsigned long long *out) {
+    __shared__ unsigned long long acc;
+    if (blockIdx.x >= n) return;
+    const uint32_t s = list[blockIdx.x];
+    if (threadIdx.x == 0) acc = 0;
+    __syncthreads();
+    unsigned long long local = 0;
+    const uint32_t o = ct.moff[s], m = ct.mn[s];
+    for (uint32_t k = threadIdx.x; k < m; k += blockDim.x) {
+        unsigned long long z = (unsigned long long)P.idx[o + k] + 0x9e3779b97f4a7c15ull;
+        z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+        z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+        local += z ^ (z >> 31);
+    }
+    atomicAdd(&acc, local);
+    __syncthreads();
+    if (threadIdx.x == 0) out[s] = acc ^ ((unsigned long long)m << 40);
 }
 
 __global__ void k_mark_members(uint32_t C, CT ct, Pool P, uint8_t *in_clump) {
@@ -1364,10 +1517,6 @@ struct Stage {
         int rc = up_list(list, d_list);
         if (rc) return rc;
         const uint32_t n = (uint32_t)list.size();
-        k_dist<<<n, 256, 0, s>>>(d_list, ct, P, tr.pos);
-        k_sort_small<<<n, 1024, 0, s>>>(d_list, ct, P);
-        c.launches += 2;
-        // segments longer than the in-block sort go through the radix sort
         std::vector<uint32_t> mn_all, mn_list;
         if (known_mn) {
             mn_list = *known_mn;
@@ -1376,6 +1525,13 @@ struct Stage {
             if (rc) return rc;
             for (uint32_t sl : list) mn_list.push_back(mn_all[sl]);
         }
+        uint32_t mx = 0;
+        for (uint32_t v : mn_list) mx = std::max(mx, v);
+        const unsigned ny = std::min(64u, std::max(1u, (mx + 8191) / 8192));
+        k_dist<<<dim3(n, ny), 256, 0, s>>>(d_list, ct, P, tr.pos);
+        k_sort_small<<<n, 1024, 0, s>>>(d_list, ct, P);
+        c.launches += 2;
+        // segments longer than the in-block sort go through the radix sort
         std::vector<uint32_t> large, base;
         uint64_t tot = 0;
         for (size_t k = 0; k < list.size(); ++k)
@@ -1908,6 +2064,8 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
         uint32_t *d_mnout = A.get<uint32_t>(nb);
         unsigned long long *d_prof = trace.on ? A.get<unsigned long long>(8 * nb) : nullptr;
         unsigned long long *reach = A.get<unsigned long long>(nb);
+        uint32_t *tent = A.get<uint32_t>(Tu);
+        unsigned long long *mhash = A.get<unsigned long long>(nb);
         if (A.failed) return kErrOutOfMemory;
         const uint32_t nlive = (uint32_t)live.size();
         // save the state (the member pool is packed first, then copied aside)
@@ -1944,11 +2102,15 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
         PLAN_CUDA(cudaMemsetAsync(dset, 0xff, nb * kDeferSlots * 4, s));
         PLAN_CUDA(cudaMemsetAsync(dover, 0, nb, s));
         PLAN_CUDA(cudaMemsetAsync(reach, 0, nb * 8, s));
+        PLAN_CUDA(cudaMemsetAsync(tent, 0xff, (size_t)Tu * 4, s));
         KTree kt = ktree_of(tr);
+        const FTree ftr{tr.phi, tr.plo, tr.nhi, tr.nlo};
+        if (!tr.phi) return kErrDevice;  // the FP32 copies are made by the density stage
         uint64_t rounds = 0, passes = 0, reruns = 0;
         // Rounds until no clump grows. Clumps in `waiting` start once every clump listed as
         // their blocker has finished (reruns in key order where their balls may meet).
         std::vector<uint8_t> finished(C, 0);
+        std::vector<uint32_t> rounds_of(C, 0);  // rounds a clump grew in during the last pass
         auto run_rounds = [&](std::vector<uint32_t> active, int seq_mode, std::vector<uint32_t> waiting,
                               const std::vector<std::vector<uint32_t>> &blockers) -> int {
             for (uint32_t sl : active) finished[sl] = 0;
@@ -1977,7 +2139,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                 k_rebind_round<<<(unsigned)active.size(), kRebindThreads, 0, s>>>(st.d_list, ct, P, kt, tr.vel, E, epos, in_clump, owner,
                                                                                   rank_of, slot_of_rank, invalid, dmax, dset, dover, seq_mode,
                                                                                   st.cp, d_grew,
-                                                                                  d_mnout, c.d_err, trace.on ? d_prof : nullptr, bc, reach);
+                                                                                  d_mnout, c.d_err, trace.on ? d_prof : nullptr, bc, reach, tent, ftr);
                 c.launches++;
                 PLAN_CUDA(cudaGetLastError());
                 std::vector<uint8_t> g;
@@ -1999,7 +2161,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                     if (r) return r;
                     k_rebind_round<<<(unsigned)retry.size(), kRebindThreads, 0, s>>>(st.d_list, ct, P, kt, tr.vel, E, epos, in_clump, owner,
                                                                                      rank_of, slot_of_rank, invalid, dmax, dset, dover, seq_mode,
-                                                                                     st.cp, d_grew, d_mnout, c.d_err, nullptr, bc, reach);
+                                                                                     st.cp, d_grew, d_mnout, c.d_err, nullptr, bc, reach, tent, ftr);
                     c.launches++;
                     PLAN_CUDA(cudaGetLastError());
                     std::vector<uint8_t> g2;
@@ -2059,8 +2221,10 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                 for (uint32_t v : grown_mn) mx = std::max<uint64_t>(mx, v);
                 c.counters[16] = std::max<uint64_t>(c.counters[16], mx);
                 if (round % 25 == 0) trace.mark("rebinding round (round, grown, largest, waiting)", round, grown.size(), mx, waiting.size());
-                for (size_t k = 0; k < active.size(); ++k)
+                for (size_t k = 0; k < active.size(); ++k) {
                     if (g[k] != 1) finished[active[k]] = 1;
+                    else rounds_of[active[k]] = round + 1;
+                }
                 admit(grown);
                 active.swap(grown);
             }
@@ -2071,11 +2235,15 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
         // reruns they met in the previous pass (PLAN_RERUN_SCHEDULE=1)
         const char *sched_env = std::getenv("PLAN_RERUN_SCHEDULE");
         const bool schedule_reruns = sched_env && *sched_env == '1';
+        const char *front_env = std::getenv("PLAN_RERUN_FRONT");  // rerun only clumps without pending partners
+        const bool front_only = front_env && *front_env == '1';
         std::vector<std::vector<uint32_t>> blockers(C);
+        std::vector<unsigned long long> pred_hash(C, 0);
         std::vector<uint32_t> active = live;
         for (uint32_t pass = 0; !active.empty(); ++pass) {
             if (pass > nlive + 2) return kErrDeviceLimit;
             ++passes;
+            const std::vector<uint32_t> active_all = active;
             std::vector<uint32_t> waiting;
             if (pass > 0 && schedule_reruns) {  // the reruns start once the reruns they met in the last pass are done
                 std::vector<uint32_t> first;
@@ -2086,8 +2254,17 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                 trace.mark("rerun schedule (rerun, start now, wait)", active.size(), first.size(), waiting.size());
                 active.swap(first);
             }
+            const std::vector<uint32_t> ran = pass > 0 ? active_all : live;
             rc = run_rounds(active, 0, waiting, (pass > 0 && schedule_reruns) ? blockers : no_blockers);
             if (rc) return rc;
+            if (!live.empty()) {  // every clump: a running one may have taken a particle from any later one
+                rc = st.up_list(live, st.d_list2);
+                if (rc) return rc;
+                k_rebind_verify<<<(unsigned)live.size(), 256, 0, s>>>(st.d_list2, (uint32_t)live.size(), ct, P, in_clump, owner, rank_of,
+                                                                      invalid, dset, dover, dmax);
+                c.launches++;
+                PLAN_CUDA(cudaGetLastError());
+            }
             std::vector<uint8_t> inv, dov;
             std::vector<uint32_t> dm, ds;
             rc = st.down(inv, invalid, C);
@@ -2095,26 +2272,73 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
             if (!rc) rc = st.down(ds, dset, (size_t)C * kDeferSlots);
             if (!rc) rc = st.down(dov, dover, C);
             if (rc) return rc;
-            uint32_t rstar = kNone;
-            for (uint32_t r = 0; r < nlive; ++r) if (inv[live[r]]) { rstar = r; break; }
-            if (rstar == kNone) break;
+            // clumps of this pass whose members differ from the prediction the others used
+            std::vector<uint8_t> changed(nlive + 1, 0);
+            if (pass > 0) {
+                rc = st.up_list(ran, st.d_list2);
+                if (rc) return rc;
+                k_member_hash<<<(unsigned)ran.size(), 256, 0, s>>>(st.d_list2, (uint32_t)ran.size(), ct, P, mhash);
+                c.launches++;
+                std::vector<unsigned long long> hnow;
+                rc = st.down(hnow, mhash, C);
+                if (rc) return rc;
+                for (uint32_t sl : ran) changed[h_rank[sl]] = hnow[sl] != pred_hash[sl];
+            }
             // rerun the invalid clumps and, in rank order, every clump that skipped particles
-            // of a clump being rerun (its holdings may change); the rest keep their result
+            // of a clump that is rerun or ended up with other members than predicted; the
+            // rest keep their result
             std::vector<uint32_t> rerun;
             std::vector<uint8_t> rr(nlive + 1, 0);
-            for (uint32_t r = rstar; r < nlive; ++r) {
-                uint32_t sl = live[r];
+            uint32_t low = kNone;  // lowest rank rerun or changed so far
+            for (uint32_t r = 0; r < nlive; ++r) {
+                const uint32_t sl = live[r];
                 bool again = inv[sl] != 0;
                 if (!again && dov[sl]) {
-                    again = dm[sl] && dm[sl] - 1 >= rstar;
+                    again = low != kNone && dm[sl] && dm[sl] - 1 >= low;
                 } else if (!again) {
                     for (int j = 0; j < kDeferSlots && !again; ++j) {
-                        uint32_t d = ds[(size_t)sl * kDeferSlots + j];
-                        again = d != kNone && d >= rstar && d < nlive && rr[d];
+                        const uint32_t d = ds[(size_t)sl * kDeferSlots + j];
+                        again = d != kNone && d < nlive && (rr[d] || changed[d]);
                     }
                 }
                 if (again) { rerun.push_back(sl); rr[r] = 1; }
+                if ((again || changed[r]) && low == kNone) low = r;
             }
+            if (rerun.empty()) break;
+            // Run only the front of the reruns: clumps none of whose recorded lower partners is
+            // itself pending. The others keep their state (and stay pending: invalid, or
+            // deferring to a pending clump) until their partners are settled; the closure above
+            // decides again after every pass, so this only avoids work that would be redone.
+            if (front_only) {
+                std::vector<uint32_t> front;
+                for (uint32_t sl : rerun) {
+                    bool ready = true;
+                    if (!dov[sl]) {
+                        for (int j = 0; j < kDeferSlots && ready; ++j) {
+                            const uint32_t d = ds[(size_t)sl * kDeferSlots + j];
+                            ready = !(d != kNone && d < nlive && rr[d] && live[d] != sl);
+                        }
+                    }
+                    if (ready) front.push_back(sl);
+                }
+                std::fill(rr.begin(), rr.end(), 0);
+                for (uint32_t sl : front) rr[h_rank[sl]] = 1;
+                trace.mark("rerun front (pending, run now)", rerun.size(), front.size());
+                rerun.swap(front);
+            }
+            // their present members are the prediction of the next pass
+            {
+                rc = st.up_list(rerun, st.d_list2);
+                if (rc) return rc;
+                k_member_hash<<<(unsigned)rerun.size(), 256, 0, s>>>(st.d_list2, (uint32_t)rerun.size(), ct, P, mhash);
+                c.launches++;
+                std::vector<unsigned long long> hnow;
+                rc = st.down(hnow, mhash, C);
+                if (rc) return rc;
+                for (uint32_t sl : rerun) pred_hash[sl] = hnow[sl];
+            }
+            trace.mark("rerun closure (invalid+deferred, changed)", rerun.size(), std::count(changed.begin(), changed.end(), 1));
+
             // blockers of each rerun clump: the rerun clumps of lower rank it met (skipped a
             // particle of, lost one to, or had one taken by); when its record overflowed, every
             // lower rerun clump whose balls came within reach
@@ -2144,7 +2368,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
             }
             reruns += rerun.size();
             PLAN_CUDA(cudaMemcpyAsync(rerun_rank, rr.data(), nlive, cudaMemcpyHostToDevice, s));
-            k_rebind_release<<<grid_for(Tu, 256), 256, 0, s>>>(Tu, owner, rerun_rank);
+            k_rebind_tentative<<<grid_for(Tu, 256), 256, 0, s>>>(Tu, owner, tent, rerun_rank);
             rc = st.up_list(rerun, st.d_list2);
             if (rc) return rc;
             k_rebind_restore<<<(unsigned)rerun.size(), 256, 0, s>>>(st.d_list2, (uint32_t)rerun.size(), ct, P, bM, bh, bri, bro, br10, br2,
