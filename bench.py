@@ -295,8 +295,10 @@ def run_gpu(args) -> None:
         total = reduce_max(ev[0].elapsed_time(ev[steps]), dist, f"cuda:{local}")
         return total, per, f.kernel_launches() - l0, dens_ms, densest_ms
 
-    for _ in range(args.warmup):
+    for w in range(args.warmup):
+        t0 = time.perf_counter()
         step(v_dev)
+        print(f"bench: warm-up step {w + 1}/{args.warmup} {time.perf_counter() - t0:.1f} s", file=sys.stderr, flush=True)
     clocks = ClockSampler(local)
     clocks.start()
     total, per, launches, dens_ms, densest_ms = timed(v_dev, args.steps)
@@ -314,9 +316,9 @@ def run_gpu(args) -> None:
     e2e_value = aggregate(world, n, args.steps, total_e2e)
     peak, peak_kind = _peaks()
     dens_avg = float(np.mean(dens_ms))
-    achieved = DENSITY_BYTES_PER_POINT * tree_points / (dens_avg / 1e3) / 1e9
+    achieved = DENSITY_BYTES_PER_POINT * tree_points / (dens_avg / 1e3) / 1e9 if dens_avg > 0 else None
     roof = {"kernel": "k_density_f (KNN + median density, FP32-filtered exact traversal)", "bound": "hbm", "achieved": achieved,
-            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_kind": f"{peak_kind} HBM copy bandwidth",
+            "peak": peak, "unit": "GB/s", "frac": achieved / peak if achieved else None, "peak_kind": f"{peak_kind} HBM copy bandwidth",
             "traffic": None, "bytes_per_unit": DENSITY_BYTES_PER_POINT, "units_per_launch": tree_points,
             "launch_ms": dens_avg}
     cpu = None
@@ -350,11 +352,11 @@ def run_gpu(args) -> None:
 def main() -> None:
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--n", type=int, default=N_FULL, help="particles per snapshot (default: the full workload)")
-    ap.add_argument("--sample-n", type=int, default=1 << 21, help="particles of the CPU sample snapshot")
+    ap.add_argument("--sample-n", type=int, default=1 << 22, help="particles of the CPU sample snapshot")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":

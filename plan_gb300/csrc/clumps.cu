@@ -1772,7 +1772,8 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
     c.counters[6] = C;
     PLAN_CUDA(cudaStreamSynchronize(s));
     double tw0 = wall_ms();
-    for (int k = 15; k < 32; ++k) c.stage_ms[k] = 0;
+    for (int k = 15; k < 32; ++k)
+        if (k != 20 && k != 21) c.stage_ms[k] = 0;  // 20, 21: the density kernels, timed before
     std::vector<uint32_t> all(C);
     std::iota(all.begin(), all.end(), 0u);
     // SortParticles + the diffuse cut after HOP (src/tree.hpp:3816-3829)
