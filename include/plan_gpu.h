@@ -165,6 +165,15 @@ int plan_knn(plan_ctx *ctx, const double *pos3, uint32_t nq, uint32_t k, double 
  * input order (3 x u32 each, low word first): order[i] receives the input index of the i-th
  * sorted key, with equal keys in the order the library's introsort leaves them. */
 int plan_morton_order(plan_ctx *ctx, const uint32_t *keys3, uint32_t n, uint32_t *order);
+/* plan_morton_order without any device allocation (no counterpart in the reference). The
+ * keys and all sort scratch live in a fixed device array inside the library, sized for at
+ * most PLAN_NOALLOC_SORT_MAX keys; larger n returns status 6 with a message. Nothing in the
+ * array has to start at zero. Calls on the same device share the array, so they must not
+ * overlap (one call at a time per device, across all contexts and threads). The first call
+ * on a device looks the array up with cudaGetSymbolAddress: make it before any stream
+ * capture on that device. */
+#define PLAN_NOALLOC_SORT_MAX 65536u
+int plan_morton_order_noalloc(plan_ctx *ctx, const uint32_t *keys3, uint32_t n, uint32_t *order);
 /* Wall time per stage of the last snapshot in milliseconds (CUDA events):
  * [0] upload+unpack, [1] ghosts, [2] keys+sort, [3] tree, [4] density KNN, [5] HOP KNN,
  * [6] grouping, [7] clump stage, [8] catalogue download. */

@@ -28,6 +28,7 @@ PLAN_ARR_NODE_U = 7
 PLAN_ARR_DENSEST = 8
 PLAN_ARR_PEAK = 9
 PLAN_ARR_SINK_COUNT = 10
+PLAN_NOALLOC_SORT_MAX = 65536
 
 STATUS = {0: "ok", 2: "argument", 3: "I/O", 4: "parameter", 5: "CUDA", 6: "out of device memory", 7: "unsupported input",
           8: "device loop limit"}
@@ -112,6 +113,7 @@ def lib() -> C.CDLL:
             "plan_stage_copy": (i32, [vp, i32, vp, C.c_size_t]),
             "plan_knn": (i32, [vp, dp, u32, u32, C.c_double, C.POINTER(C.c_uint32), dp]),
             "plan_morton_order": (i32, [vp, vp, u32, vp]),
+            "plan_morton_order_noalloc": (i32, [vp, vp, u32, vp]),
             "plan_stage_times": (i32, [vp, dp, i32]),
             "plan_kernel_launches": (u64, [vp]),
             "plan_counters": (i32, [vp, C.POINTER(C.c_uint64), i32]),
@@ -133,7 +135,7 @@ EXPORTED = [
     "plan_lis_time", "plan_lis_get_view", "plan_ctx_create", "plan_ctx_destroy", "plan_last_error", "plan_footprint_bytes",
     "plan_build_tree", "plan_find_planetesimals", "plan_find_clumps", "plan_catalogue_free", "plan_catalogue_count",
     "plan_catalogue_get", "plan_catalogue_summary", "plan_catalogue_write_peaks", "plan_catalogue_basic_results",
-    "plan_stage_count", "plan_stage_copy", "plan_knn", "plan_morton_order", "plan_stage_times", "plan_kernel_launches", "plan_counters",
+    "plan_stage_count", "plan_stage_copy", "plan_knn", "plan_morton_order", "plan_morton_order_noalloc", "plan_stage_times", "plan_kernel_launches", "plan_counters",
     "plan_synth_default_spec", "plan_synth_records", "plan_synth_write_lis", "plan_synth_four_pi_G_for_mean",
 ]
 
@@ -317,6 +319,15 @@ class Finder:
         k = np.ascontiguousarray(keys3, dtype=np.uint32).reshape(-1, 3)
         out = np.empty(len(k), dtype=np.uint32)
         rc = lib().plan_morton_order(self._h, k.ctypes.data, len(k), out.ctypes.data)
+        if rc:
+            raise PlanError(rc, self.error())
+        return out
+
+    def morton_order_noalloc(self, keys3: np.ndarray) -> np.ndarray:
+        """morton_order without device allocation (at most PLAN_NOALLOC_SORT_MAX keys)."""
+        k = np.ascontiguousarray(keys3, dtype=np.uint32).reshape(-1, 3)
+        out = np.empty(len(k), dtype=np.uint32)
+        rc = lib().plan_morton_order_noalloc(self._h, k.ctypes.data, len(k), out.ctypes.data)
         if rc:
             raise PlanError(rc, self.error())
         return out

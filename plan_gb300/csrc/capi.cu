@@ -14,6 +14,12 @@ namespace plan {
 
 thread_local Context *g_ctx = nullptr;
 
+// The fixed device array of plan_morton_order_noalloc: the keys (4 x u32 per key) and the sort
+// scratch of up to PLAN_NOALLOC_SORT_MAX keys. Nothing in it has to start at zero (every call
+// writes what it later reads); calls on one device share it and must not overlap.
+constexpr size_t kNoAllocBytes = 6u << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
 int set_cuda_error(cudaError_t e, const char *what, const char *file, int line) {
     if (g_ctx) {
         char buf[512];
@@ -298,6 +304,50 @@ int plan_morton_order(plan_ctx *h, const uint32_t *keys3, uint32_t n, uint32_t *
     if (scr) cudaFreeAsync(scr, s);
     if (cudaStreamSynchronize(s) != cudaSuccess && !rc) rc = kErrDevice;
     return c.status_from(rc, "plan_morton_order");
+}
+
+int plan_morton_order_noalloc(plan_ctx *h, const uint32_t *keys3, uint32_t n, uint32_t *order) {
+    if (!h || (n && (!keys3 || !order))) return kErrArgument;
+    Context &c = h->c;
+    g_ctx = &c;
+    c.last_error.clear();
+    cudaSetDevice(c.device);
+    if (n == 0) return kOk;
+    if (n > PLAN_NOALLOC_SORT_MAX) {
+        c.last_error = "plan_morton_order_noalloc: " + std::to_string(n) + " keys exceed the fixed limit of " +
+                       std::to_string(PLAN_NOALLOC_SORT_MAX);
+        return kErrOutOfMemory;
+    }
+    const size_t key_bytes = (4 * (size_t)n * 4 + 255) & ~size_t(255), sb = morton_sort_scratch_bytes(n);
+    if (key_bytes + sb > kNoAllocBytes) {
+        c.last_error = "plan_morton_order_noalloc: the fixed device array is too small for " + std::to_string(n) + " keys";
+        return kErrOutOfMemory;
+    }
+    if (!c.noalloc_scratch) {  // this device's copy of the array, looked up once
+        cudaError_t e = cudaGetSymbolAddress(&c.noalloc_scratch, g_noalloc_scratch);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            c.noalloc_scratch = nullptr;
+            c.last_error = std::string("plan_morton_order_noalloc: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e);
+            return kErrDevice;
+        }
+    }
+    cudaStream_t s = c.stream;
+    std::vector<uint32_t> w(4 * (size_t)n);
+    for (uint32_t i = 0; i < n; ++i) {
+        w[i] = keys3[3 * (size_t)i];
+        w[(size_t)n + i] = keys3[3 * (size_t)i + 1];
+        w[2 * (size_t)n + i] = keys3[3 * (size_t)i + 2];
+        w[3 * (size_t)n + i] = i;
+    }
+    uint32_t *d = static_cast<uint32_t *>(c.noalloc_scratch);
+    void *scr = static_cast<unsigned char *>(c.noalloc_scratch) + key_bytes;
+    int rc = kOk;
+    if (cudaMemcpyAsync(d, w.data(), w.size() * 4, cudaMemcpyHostToDevice, s) != cudaSuccess) rc = kErrDevice;
+    if (!rc) rc = morton_sort_std(c, d, d + n, d + 2 * (size_t)n, d + 3 * (size_t)n, n, scr, sb, s);
+    if (!rc && cudaMemcpyAsync(order, d + 3 * (size_t)n, (size_t)n * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess) rc = kErrDevice;
+    if (cudaStreamSynchronize(s) != cudaSuccess && !rc) rc = kErrDevice;
+    return c.status_from(rc, "plan_morton_order_noalloc");
 }
 
 int plan_stage_times(const plan_ctx *h, double *ms, int n) {

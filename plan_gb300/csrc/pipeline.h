@@ -85,6 +85,7 @@ struct Context {
     FindScalars fs{};
     uint32_t *densest = nullptr, *peak = nullptr;  // stage arrays of the last finder run
     cudaEvent_t kev[2] = {nullptr, nullptr};        // brackets one kernel for its timing
+    void *noalloc_scratch = nullptr;                // this device's fixed array (plan_morton_order_noalloc)
     int status_from(int rc, const char *what);
     // grow an arena (contents are discarded) to at least `bytes`
     int ensure(Arena &a, size_t bytes);
