@@ -1105,6 +1105,9 @@ std::string Finder::find(uint32_t num_in) {
     del.clear();
     num_planetesimals = (uint32_t)clumps.size();
     std::ostringstream out;
+    // the reference formats this line on a stream it shares with WriteBasicResults, which
+    // leaves it in scientific notation after the first snapshot (src/tree.hpp:4322, 4943)
+    if (stream_scientific) out << std::scientific;
     out << "Finish clump finding for t = " << time << ", ";
     phase_mark("prune+rip+ghost");
     // 10. angular momentum and ranking, src/tree.hpp:4273-4326

@@ -202,6 +202,7 @@ struct Finder {
 
     // FindPlanetesimals (src/tree.hpp:3576-4339). Returns the summary line.
     std::string find(uint32_t num_particles_in);
+    bool stream_scientific = false;  // the summary stream's state after an earlier snapshot
     double density_kernel(const Heap &heap, uint32_t self, unsigned k) const;
     double pow15(double x) const;
     double hill_pow(double x) const;

@@ -110,6 +110,7 @@ int main(int argc, char **argv) {
         f.threads = nthreads;
         f.pow_mode = pow_mode ? POW_CORRECT : POW_LIBM;
         f.time = snap.time;
+        f.stream_scientific = !first;
         f.tree.build(par, snap.parts, true);
         double t2 = now();
         std::string summary = f.find(nin);

@@ -183,7 +183,7 @@ int main(int argc, char **argv) {
     std::ostringstream oc;  // keeps its formatting state across snapshots, as the reference's
     bool first = true;
     int status = 0;
-    for (int num = start_num; num != end_num + interval && num_files > 0; num += interval) {
+    for (int num = start_num; num <= end_num && num_files > 0; num += interval) {  // mpi->loop_begin..loop_end
         std::ostringstream nn;
         nn << std::setw(4) << std::setfill('0') << num;
         std::vector<std::string> files;

@@ -55,6 +55,8 @@ CASES = [
     Case("config1_262k", 1, 262144, 1, 128),
 ]
 BY_NAME = {c.name: c for c in CASES}
+# one run over two snapshot files (-f 0:1): the second is later in time and uses the first's box
+MULTI = [Case("multi_0", 1, 20000, 5, 32), Case("multi_1", 1, 20000, 6, 32, time=0.25)]
 
 
 def _records(c: Case):

@@ -110,10 +110,46 @@ def oracle_cr(m: dict) -> dict:
             "max_rel_density_cr_diff": rel}
 
 
+def multi_snapshot() -> None:
+    """Two snapshots in one run (-f 0:1, the second at t = 0.25): the reference's summary
+    stream keeps the scientific notation WriteBasicResults leaves on it, and the second file
+    takes the box and masses of the first."""
+    with tempfile.TemporaryDirectory() as tmp:
+        tmp = Path(tmp)
+        shas = []
+        for k, c in enumerate(cases.MULTI):
+            m = cases.materialise(c, tmp / f"c{k}")
+            dst = tmp / "in" / f"Snap.{k:04d}.ds.lis"
+            dst.parent.mkdir(exist_ok=True)
+            shutil.copy(m["lis"][0], dst)
+            shas.append(m["sha256"][0])
+            if k == 0:
+                shutil.copy(m["param"], tmp / "in" / "para.txt")
+        out = tmp / "ref"
+        out.mkdir()
+        args = ["-c", "1", "-i", str(tmp / "in"), "-b", "Snap", "-p", "ds", "-f", "0:1", "-o", str(out / "res.txt"), "-t",
+                str(tmp / "in" / "para.txt"), "--Combined"]
+        r = subprocess.run([str(REF)] + args, cwd=out, capture_output=True, text=True, check=True)
+        g = HERE / "multi_snapshot"
+        if g.exists():
+            shutil.rmtree(g)
+        g.mkdir()
+        peaks = sorted(out.glob("peaks_at_*.txt"))
+        for pk in peaks:
+            shutil.copy(pk, g / pk.name)
+        shutil.copy(out / "res_planetesimals.txt", g / "planetesimals.txt")
+        summary = [ln for ln in r.stdout.splitlines() if "Finish clump finding" in ln]
+        meta = {"lis_sha256": shas, "summary": summary, "peaks_files": [pk.name for pk in peaks]}
+        (g / "meta.json").write_text(json.dumps(meta, indent=1) + "\n")
+        print("multi_snapshot:", *summary, sep="\n  ")
+
+
 def main() -> None:
     if not REF.exists():
         sys.exit(f"{REF} missing: run `make -C oracle ref` in a checkout with the reference")
     only = set(sys.argv[1:])
+    if not only or "multi_snapshot" in only:
+        multi_snapshot()
     for c in cases.CASES:
         if only and c.name not in only:
             continue

@@ -191,3 +191,25 @@ def test_large_snapshot_against_oracle(n, seed, pg, finder, tmp_path):
     assert len(cat) > 0
     cat.close()
     snap.close()
+
+
+def test_cli_two_snapshots(pg, tmp_path):
+    """The drop-in binary over two snapshots in one run writes the reference's files and
+    summary lines (second file: box and masses of the first, scientific summary stream)."""
+    import json
+
+    from test_oracle_golden import _multi_inputs, multi_snapshot_args
+
+    g = GOLDEN / "multi_snapshot"
+    meta = json.loads((g / "meta.json").read_text())
+    d, shas = _multi_inputs(tmp_path)
+    assert shas == meta["lis_sha256"]
+    out = tmp_path / "out"
+    out.mkdir()
+    cli = ROOT / "plan_gb300" / "lib" / "plan_gpu"
+    r = subprocess.run([str(cli)] + multi_snapshot_args(d, out), cwd=out, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert [ln for ln in r.stdout.splitlines() if "Finish clump finding" in ln] == meta["summary"]
+    for name in meta["peaks_files"]:
+        assert (out / name).read_bytes() == (g / name).read_bytes()
+    assert (out / "res_planetesimals.txt").read_bytes() == (g / "planetesimals.txt").read_bytes()

@@ -95,3 +95,43 @@ def test_oracle_morton_order_distinct_keys(oracle_mod):
     k[:, 2] &= 0xF
     order = oracle_mod.morton_order(k)
     np.testing.assert_array_equal(order, np.lexsort((k[:, 0], k[:, 1], k[:, 2])))
+
+
+def _multi_inputs(tmp_path):
+    import shutil
+
+    d = tmp_path / "in"
+    d.mkdir()
+    shas = []
+    for k, c in enumerate(cases.MULTI):
+        m = cases.materialise(c, tmp_path / f"c{k}")
+        shutil.copy(m["lis"][0], d / f"Snap.{k:04d}.ds.lis")
+        shas.append(m["sha256"][0])
+        if k == 0:
+            shutil.copy(m["param"], d / "para.txt")
+    return d, shas
+
+
+def multi_snapshot_args(d, out):
+    return ["-c", "1", "-i", str(d), "-b", "Snap", "-p", "ds", "-f", "0:1", "-o", str(out / "res.txt"), "-t", str(d / "para.txt"),
+            "--Combined"]
+
+
+def test_oracle_cli_two_snapshots(oracle_mod, tmp_path):
+    """One run over two snapshots (src/main.cpp:64-83): the second summary line keeps the
+    scientific notation of the reference's shared stream; the files equal the reference's."""
+    import json
+    import subprocess
+
+    g = GOLDEN / "multi_snapshot"
+    meta = json.loads((g / "meta.json").read_text())
+    d, shas = _multi_inputs(tmp_path)
+    assert shas == meta["lis_sha256"]
+    out = tmp_path / "out"
+    out.mkdir()
+    cli = oracle_mod.CLI
+    r = subprocess.run([str(cli)] + multi_snapshot_args(d, out), cwd=out, capture_output=True, text=True, check=True)
+    assert [ln for ln in r.stdout.splitlines() if "Finish clump finding" in ln] == meta["summary"]
+    for name in meta["peaks_files"]:
+        assert (out / name).read_bytes() == (g / name).read_bytes()
+    assert (out / "res_planetesimals.txt").read_bytes() == (g / "planetesimals.txt").read_bytes()
