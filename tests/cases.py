@@ -55,6 +55,14 @@ CASES = [
     Case("config1_262k", 1, 262144, 1, 128),
 ]
 BY_NAME = {c.name: c for c in CASES}
+# command-line and parameter variants of one snapshot: (name, case, extra arguments)
+VARIANTS = [
+    ("w1_20k_parlist_s3", Case("w1_20k", 1, 20000, 5, 32), ["--Save_Clumps", "-s", "3"]),
+    ("w1_20k_num_peaks5", Case("w1_20k_num_peaks5", 1, 20000, 5, 32, extra={"num_peaks": 5}), ["--Save_Clumps"]),
+    ("w1_20k_no_ghost", Case("w1_20k", 1, 20000, 5, 32), ["--No_Ghost", "--Save_Clumps"]),
+    ("w1_20k_diffuse_hill", Case("w1_20k_dh", 1, 20000, 5, 32, extra={"clump_diffuse_threshold": 0.45, "Hill_fraction_for_merge": 0.4}),
+     ["--Save_Clumps"]),
+]
 # one run over two snapshot files (-f 0:1): the second is later in time and uses the first's box
 MULTI = [Case("multi_0", 1, 20000, 5, 32), Case("multi_1", 1, 20000, 6, 32, time=0.25)]
 

@@ -144,12 +144,38 @@ def multi_snapshot() -> None:
         print("multi_snapshot:", *summary, sep="\n  ")
 
 
+def variants() -> None:
+    """Command-line and parameter variants of one snapshot, run by the reference's CLI."""
+    for name, c, extra in cases.VARIANTS:
+        with tempfile.TemporaryDirectory() as tmp:
+            tmp = Path(tmp)
+            m = cases.materialise(c, tmp / "in")
+            out = tmp / "ref"
+            out.mkdir()
+            r = subprocess.run([str(REF)] + cases.cli_args(m, str(out / "res.txt")) + extra, cwd=out, capture_output=True, text=True,
+                               check=True)
+            g = HERE / name
+            if g.exists():
+                shutil.rmtree(g)
+            g.mkdir()
+            pk = cases.find_peaks_file(out)
+            shutil.copy(pk, g / pk.name)
+            shutil.copy(out / "res_planetesimals.txt", g / "planetesimals.txt")
+            summary = [ln for ln in r.stdout.splitlines() if "Finish clump finding" in ln]
+            meta = {"case": name, "lis_sha256": m["sha256"], "args": extra, "summary": summary[0].strip(), "peaks_file": pk.name,
+                    "parlist": cases.parlist_digests(out)}
+            (g / "meta.json").write_text(json.dumps(meta, indent=1) + "\n")
+            print(f"{name}: {meta['summary']} ({len(meta['parlist'])} member lists)")
+
+
 def main() -> None:
     if not REF.exists():
         sys.exit(f"{REF} missing: run `make -C oracle ref` in a checkout with the reference")
     only = set(sys.argv[1:])
     if not only or "multi_snapshot" in only:
         multi_snapshot()
+    if not only or "variants" in only:
+        variants()
     for c in cases.CASES:
         if only and c.name not in only:
             continue

@@ -135,3 +135,25 @@ def test_oracle_cli_two_snapshots(oracle_mod, tmp_path):
     for name in meta["peaks_files"]:
         assert (out / name).read_bytes() == (g / name).read_bytes()
     assert (out / "res_planetesimals.txt").read_bytes() == (g / "planetesimals.txt").read_bytes()
+
+
+@pytest.mark.parametrize("name,case,extra", cases.VARIANTS, ids=[v[0] for v in cases.VARIANTS])
+def test_oracle_cli_variants(name, case, extra, oracle_mod, tmp_path):
+    """Sub-sampled member lists (-s), the num_peaks cap, --No_Ghost and the merge parameters
+    (src/global.cpp:247-289, src/tree.hpp:4302-4316, 5191-5222): the oracle's files equal
+    the reference's."""
+    import json
+    import subprocess
+
+    g = GOLDEN / name
+    meta = json.loads((g / "meta.json").read_text())
+    m = cases.materialise(case, tmp_path / "in")
+    assert m["sha256"] == meta["lis_sha256"]
+    out = tmp_path / "out"
+    out.mkdir()
+    r = subprocess.run([str(oracle_mod.CLI)] + cases.cli_args(m, str(out / "res.txt")) + extra, cwd=out, capture_output=True, text=True,
+                       check=True)
+    assert meta["summary"] in r.stdout
+    assert (out / meta["peaks_file"]).read_bytes() == (g / meta["peaks_file"]).read_bytes()
+    assert (out / "res_planetesimals.txt").read_bytes() == (g / "planetesimals.txt").read_bytes()
+    assert cases.parlist_digests(out) == meta["parlist"]
