@@ -910,6 +910,7 @@ __device__ void defer_add(uint32_t *dset, uint8_t *dover, uint32_t *dmax, uint32
 // later clump, which is then invalid. A clump that loses q to an earlier one is invalid.
 // Invalid clumps are restored and rerun by the host until none is left; the clumps below
 // the lowest invalid rank are final after every pass, so this ends.
+template <int kSpec>
 __global__ void __launch_bounds__(kRebindThreads) k_rebind_round(const uint32_t *list, CT ct, Pool P, KTree t, const double4_32a *vel,
                                                                  const uint32_t *E, const uint32_t *epos, uint8_t *in_clump, uint32_t *owner,
                                                                  const uint32_t *rank_of, const uint32_t *slot_of_rank, uint8_t *invalid,
@@ -1135,7 +1136,112 @@ __global__ void __launch_bounds__(kRebindThreads) k_rebind_round(const uint32_t 
             tf[i] = cf;
         }
         __syncthreads();
-        if (threadIdx.x < 32) {
+        if (kSpec && threadIdx.x < 32) {
+            // Speculative windows, exact by verification: decide 32 candidates against the
+            // window's first state, run the FP64 update chain through the tentative
+            // acceptances only, then check every decision against the exact state before it.
+            // Everything before the first disagreement is the reference's sequence; the first
+            // disagreeing candidate is decided by its (exact) check.
+            __shared__ double sst[33][7];  // M and the six components after each tentative acceptance
+            const int lane = threadIdx.x;
+            const unsigned full = 0xffffffffu;
+            const int cl = lane < 6 ? lane : 0;  // the state component this lane carries
+            uint32_t at = s_at;
+            while (at < tend) {
+                ++iters;
+                const uint32_t k = at + lane;
+                const bool valid = k < tend;
+                const bool tk = valid && ttaken[k - base] != 0;
+                bool tent = false;
+                if (valid && !tk) {
+                    const int r = bound_hilo(tf[k - base], Mf, sh, sl, G32, shear32);
+                    tent = r >= 0 ? r == 1 : bound_fp64(tpos[k - base], tvel[k - base], M_, x_, y_, z_, vx_, vy_, vz_, cp);
+                }
+                const unsigned B = __ballot_sync(full, tent), V = __ballot_sync(full, valid);
+                const uint32_t wend = min(at + 32, tend);
+                if (!B) {
+                    at = wend;
+                    continue;
+                }
+                // states after each tentative acceptance (src/tree.hpp:4696-4701)
+                double Mi = M_;
+                double ci = cl == 0 ? x_ : cl == 1 ? y_ : cl == 2 ? z_ : cl == 3 ? vx_ : cl == 4 ? vy_ : vz_;
+                if (lane < 6) sst[0][1 + lane] = ci;
+                if (lane == 0) sst[0][0] = Mi;
+                int ns = 0;
+                for (unsigned bits = B; bits; bits &= bits - 1u) {
+                    const uint32_t j = at + (uint32_t)(__ffs(bits) - 1) - base;
+                    const double4_32a p = tpos[j], v = tvel[j];
+                    const double Mn = Mi + p.w;
+                    const double qc = cl == 0 ? p.x : cl == 1 ? p.y : cl == 2 ? p.z : cl == 3 ? v.x : cl == 4 ? v.y : v.z;
+                    ci = (ci * Mn + p.w * qc) / Mn;
+                    Mi = Mn;
+                    ++ns;
+                    if (lane < 6) sst[ns][1 + lane] = ci;
+                    if (lane == 0) sst[ns][0] = Mi;
+                }
+                __syncwarp();
+                bool ver = false;
+                if (valid && !tk) {
+                    const int nb = __popc(B & ((1u << lane) - 1u));
+                    const double Ms = sst[nb][0];
+                    const double s0 = sst[nb][1], s1 = sst[nb][2], s2 = sst[nb][3], s3 = sst[nb][4], s4 = sst[nb][5], s5 = sst[nb][6];
+                    float h[6], l[6];
+                    split_f(s0, h[0], l[0]); split_f(s1, h[1], l[1]); split_f(s2, h[2], l[2]);
+                    split_f(s3, h[3], l[3]); split_f(s4, h[4], l[4]); split_f(s5, h[5], l[5]);
+                    const int r = bound_hilo(tf[k - base], (float)Ms, h, l, G32, shear32);
+                    ver = r >= 0 ? r == 1 : bound_fp64(tpos[k - base], tvel[k - base], Ms, s0, s1, s2, s3, s4, s5, cp);
+                }
+                const unsigned Vb = __ballot_sync(full, ver);
+                const unsigned mism = (Vb ^ B) & V;
+                unsigned accepted = B;
+                int nstate = ns;
+                int extra = -1;  // a candidate accepted by its check beyond the chain's states
+                uint32_t next = wend;
+                if (mism) {
+                    const int m = __ffs(mism) - 1;
+                    const unsigned below = (1u << m) - 1u;
+                    accepted = (B & below) | (Vb & (1u << m));
+                    nstate = __popc(B & below);
+                    if ((Vb >> m) & 1u) extra = m;
+                    next = at + (uint32_t)m + 1;
+                }
+                double M2 = sst[nstate][0];
+                double c2 = sst[nstate][1 + cl];
+                if (extra >= 0) {
+                    const uint32_t j = at + (uint32_t)extra - base;
+                    const double4_32a p = tpos[j], v = tvel[j];
+                    const double Mn = M2 + p.w;
+                    const double qc = cl == 0 ? p.x : cl == 1 ? p.y : cl == 2 ? p.z : cl == 3 ? v.x : cl == 4 ? v.y : v.z;
+                    c2 = (c2 * Mn + p.w * qc) / Mn;
+                    M2 = Mn;
+                }
+                __syncwarp();
+                float rh, rl;
+                split_f(c2, rh, rl);
+                for (int q = 0; q < 6; ++q) {
+                    sh[q] = __shfl_sync(full, rh, q);
+                    sl[q] = __shfl_sync(full, rl, q);
+                }
+                x_ = __shfl_sync(full, c2, 0);
+                y_ = __shfl_sync(full, c2, 1);
+                z_ = __shfl_sync(full, c2, 2);
+                vx_ = __shfl_sync(full, c2, 3);
+                vy_ = __shfl_sync(full, c2, 4);
+                vz_ = __shfl_sync(full, c2, 5);
+                M_ = M2;
+                Mf = (float)M2;
+                if ((accepted >> lane) & 1u) {  // each accepted lane claims its own candidate
+                    const uint32_t q2 = tq[k - base];
+                    if (seq_mode) in_clump[q2] = 1;
+                    else atomicMin(&owner[q2], myrank);
+                    acc[nacc_ + __popc(accepted & ((1u << lane) - 1u))] = q2;
+                }
+                nacc_ += __popc(accepted);
+                at = next;
+            }
+            if (lane == 0) s_at = at;
+        } else if (threadIdx.x < 32) {
             const int lane = threadIdx.x;
             uint32_t at = s_at;
             while (at < tend) {
@@ -2107,6 +2213,10 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
         KTree kt = ktree_of(tr);
         const FTree ftr{tr.phi, tr.plo, tr.nhi, tr.nlo};
         if (!tr.phi) return kErrDevice;  // the FP32 copies are made by the density stage
+        // speculative acceptance windows (exact by verification; PLAN_ACCEPT_SPECULATE=1)
+        const char *spec_env = std::getenv("PLAN_ACCEPT_SPECULATE");
+        const bool speculate = spec_env && *spec_env == '1';
+        auto rebind_kernel = speculate ? k_rebind_round<1> : k_rebind_round<0>;
         uint64_t rounds = 0, passes = 0, reruns = 0;
         // Rounds until no clump grows. Clumps in `waiting` start once every clump listed as
         // their blocker has finished (reruns in key order where their balls may meet).
@@ -2137,7 +2247,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                 int r = st.up_list(active, st.d_list);
                 if (r) return r;
                 double t_a = wall_ms();
-                k_rebind_round<<<(unsigned)active.size(), kRebindThreads, 0, s>>>(st.d_list, ct, P, kt, tr.vel, E, epos, in_clump, owner,
+                rebind_kernel<<<(unsigned)active.size(), kRebindThreads, 0, s>>>(st.d_list, ct, P, kt, tr.vel, E, epos, in_clump, owner,
                                                                                   rank_of, slot_of_rank, invalid, dmax, dset, dover, seq_mode,
                                                                                   st.cp, d_grew,
                                                                                   d_mnout, c.d_err, trace.on ? d_prof : nullptr, bc, reach, tent, ftr);
@@ -2160,7 +2270,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                     r = st.maybe_compact(true);
                     if (!r) r = st.up_list(retry, st.d_list);
                     if (r) return r;
-                    k_rebind_round<<<(unsigned)retry.size(), kRebindThreads, 0, s>>>(st.d_list, ct, P, kt, tr.vel, E, epos, in_clump, owner,
+                    rebind_kernel<<<(unsigned)retry.size(), kRebindThreads, 0, s>>>(st.d_list, ct, P, kt, tr.vel, E, epos, in_clump, owner,
                                                                                      rank_of, slot_of_rank, invalid, dmax, dset, dover, seq_mode,
                                                                                      st.cp, d_grew, d_mnout, c.d_err, nullptr, bc, reach, tent, ftr);
                     c.launches++;
