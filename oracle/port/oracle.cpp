@@ -585,13 +585,22 @@ uint32_t Tree::ball_count(const V3 &c, double r) const {
     return (uint32_t)v.size();
 }
 
-double Tree::quadratic_spline(V3 dist) const {  // src/tree.hpp:3406-3419
+// src/tree.hpp:3406-3419. The reference writes std::pow(v, 2.); its optimised build (GCC,
+// -O2 and above) turns that call into v * v, the correctly rounded square, so that is what
+// it computes (glibc's pow(v, 2.) itself differs from v * v by one unit in the last place on
+// about one argument in a thousand).
+double Tree::quadratic_spline(V3 dist) const {
     for (int d = 0; d < 3; ++d) dist[d] = std::fabs(dist[d]);
     double w = 1;
     for (int i = 0; i < 3; ++i) {
-        if (dist[i] <= half_cell_length[i]) w *= (0.75 - dist[i] * dist[i] / cell_length_squared[i]);
-        else if (dist[i] < three_half_cell_length[i]) w *= 0.5 * std::pow(1.5 - dist[i] / cell_length[i], 2.);
-        else return 0.;
+        if (dist[i] <= half_cell_length[i]) {
+            w *= (0.75 - dist[i] * dist[i] / cell_length_squared[i]);
+        } else if (dist[i] < three_half_cell_length[i]) {
+            const double v = 1.5 - dist[i] / cell_length[i];
+            w *= 0.5 * (v * v);
+        } else {
+            return 0.;
+        }
     }
     return w;
 }

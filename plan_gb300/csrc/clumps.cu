@@ -1786,11 +1786,10 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
     uint32_t horiz = p.box_resolution[0] * p.box_resolution[1];
     if (tr.box.half_width < p.max_half_width + p.max_ghost_zone_width - 1e-16)
         horiz = (uint32_t)std::pow(tr.box.half_width / p.cell_length[0] * ((tr.box.half_width - p.max_ghost_zone_width) / tr.box.half_width), 2.0);
-    if (!(N >= 4 * horiz)) {
-        c.last_error = "fewer than 4 particles per horizontal cell: the spline density kernel of the reference is not built yet";
-        return kErrUnsupported;
-    }
-    if (!p.fixed_hop && N >= 1.67e7) p.hop = 64;
+    // at least 4 particles per horizontal cell: median-sphere density; otherwise the spline
+    // kernel, and groups are pruned right after HOP (src/tree.hpp:3583-3610, 3834-3836)
+    const bool median = N >= 4 * horiz;
+    if (median && !p.fixed_hop && N >= 1.67e7) p.hop = 64;
     const double PI = 3.14159265358979323846;
     double thr = std::pow(p.Omega, 2.) / PI / p.grav_constant * 2.;
     if (p.mass_total_code_units / N / p.cell_volume > thr / 4) thr *= 9. / 8.;
@@ -1807,7 +1806,8 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
         c.last_error = "knn and hop must lie in [1, 128] and not exceed the number of tree points";
         return kErrUnsupported;
     }
-    c.fs = FindScalars{thr, 3 * thr, p.min_trusted_mass, diffuse, hillf, p.knn, p.hop, 1};
+    c.fs = FindScalars{thr, 3 * thr, p.min_trusted_mass, diffuse, hillf, p.knn, p.hop, median ? 1 : 0,
+                       spline_cells(p.cell_length, p.cell_volume)};
 
     // 1-2. densities and densest neighbours
     int rc = launch_density(c, p, p.knn, s);
@@ -1894,6 +1894,17 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
         std::vector<uint8_t> alive(C, 1);
         for (uint32_t i = 0; i < C; ++i) if (too[i]) alive[i] = 0;
         PLAN_CUDA(cudaMemcpyAsync(ct.alive, alive.data(), C, cudaMemcpyHostToDevice, s));
+    }
+    if (!median && C) {  // RemoveSmallMassAndLowPeak (src/tree.hpp:3834-3836)
+        k_prune<<<grid_for(C, 128), 128, 0, s>>>(C, ct, P, tr.vel, tr.dens, st.cp, st.d_flag8);
+        c.launches++;
+        std::vector<uint8_t> kill, alive;
+        rc = st.down(kill, st.d_flag8, C);
+        if (!rc) rc = st.down(alive, ct.alive, C);
+        if (rc) return rc;
+        for (uint32_t i = 0; i < C; ++i) if (kill[i]) alive[i] = 0;
+        PLAN_CUDA(cudaMemcpyAsync(ct.alive, alive.data(), C, cudaMemcpyHostToDevice, s));
+        trace.mark("small-mass and low-peak groups removed");
     }
     std::vector<uint32_t> live;
     rc = st.live_order(live);

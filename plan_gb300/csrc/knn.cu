@@ -84,9 +84,9 @@ __global__ void __launch_bounds__(128) k_knn_positions(KTree t, const double *q3
 }
 
 
-template <int KMAX>
+template <int KMAX, int SPL>
 __global__ void __launch_bounds__(128) k_density_at(KTree t, const double *q3, const double *est, uint32_t nq, uint32_t k,
-                                                    double four_pi_over_three, double *out, unsigned *err) {
+                                                    double four_pi_over_three, SplineCells sc, double *out, unsigned *err) {
     extern __shared__ unsigned char smem[];
     double *sd = reinterpret_cast<double *>(smem);
     uint32_t *si = reinterpret_cast<uint32_t *>(sd + KMAX * blockDim.x);
@@ -96,7 +96,15 @@ __global__ void __launch_bounds__(128) k_density_at(KTree t, const double *q3, c
     double qx = q3[3 * i], qy = q3[3 * i + 1], qz = q3[3 * i + 2];
     double r = est[i] != 0 ? est[i] : knn_first_radius(t, qx, qy, qz, 0xffffffffu, k, err);
     int got = knn_query(t, qx, qy, qz, r, k, h, err);
-    out[i] = got == (int)k ? knn_median_density(t, h, (int)k, four_pi_over_three) : 0.0;
+    if (got != (int)k) {
+        out[i] = 0.0;
+    } else if constexpr (SPL) {
+        // the reference passes self_id = 0: offsets are taken from tree point 0 (src/tree.hpp:4889, 4905)
+        const double4_32a p0 = t.pos[0];
+        out[i] = spline_density(t.pos, [&](int j) { return h.iget(j); }, (int)k, p0.x, p0.y, p0.z, sc);
+    } else {
+        out[i] = knn_median_density(t, h, (int)k, four_pi_over_three);
+    }
 }
 
 // ---------------------------------------------------------------- FP32-filtered kernels
@@ -131,9 +139,9 @@ __device__ __forceinline__ double f_median_density(const KTree &t, const double 
     return dens / (fpo3 * cr_pow15(r2));
 }
 
-template <int CAP>
-__global__ void __launch_bounds__(128) k_density_f(KTree t, FTree f, uint32_t n, uint32_t k, double fpo3, double *dens, uint32_t *redo,
-                                                   uint32_t *nredo, unsigned *err) {
+template <int CAP, int SPL>
+__global__ void __launch_bounds__(128) k_density_f(KTree t, FTree f, uint32_t n, uint32_t k, double fpo3, SplineCells sc, double *dens,
+                                                   uint32_t *redo, uint32_t *nredo, unsigned *err) {
     extern __shared__ unsigned char smem[];
     float *sk = reinterpret_cast<float *>(smem);
     uint32_t *si = reinterpret_cast<uint32_t *>(sk + CAP * blockDim.x);
@@ -149,7 +157,8 @@ __global__ void __launch_bounds__(128) k_density_f(KTree t, FTree f, uint32_t n,
         redo[atomicAdd(nredo, 1u)] = i;
         return;
     }
-    dens[i] = f_median_density(t, d64, i64, (int)k, fpo3);
+    if constexpr (SPL) dens[i] = spline_density(t.pos, [&](int j) { return i64[j]; }, (int)k, q.x, q.y, q.z, sc);
+    else dens[i] = f_median_density(t, d64, i64, (int)k, fpo3);
 }
 
 template <int CAP>
@@ -185,9 +194,9 @@ __global__ void __launch_bounds__(128) k_densest_f(KTree t, FTree f, uint32_t n,
 }
 
 // exact FP64 path for a list of queries
-template <int KMAX>
-__global__ void __launch_bounds__(128) k_density_list(KTree t, const uint32_t *list, uint32_t n, uint32_t k, double fpo3, double *dens,
-                                                      unsigned *err) {
+template <int KMAX, int SPL>
+__global__ void __launch_bounds__(128) k_density_list(KTree t, const uint32_t *list, uint32_t n, uint32_t k, double fpo3, SplineCells sc,
+                                                      double *dens, unsigned *err) {
     extern __shared__ unsigned char smem[];
     double *sd = reinterpret_cast<double *>(smem);
     uint32_t *si = reinterpret_cast<uint32_t *>(sd + KMAX * blockDim.x);
@@ -203,7 +212,8 @@ __global__ void __launch_bounds__(128) k_density_list(KTree t, const uint32_t *l
         dens[i] = 0;
         return;
     }
-    dens[i] = knn_median_density(t, h, (int)k, fpo3);
+    if constexpr (SPL) dens[i] = spline_density(t.pos, [&](int jj) { return h.iget(jj); }, (int)k, q.x, q.y, q.z, sc);
+    else dens[i] = knn_median_density(t, h, (int)k, fpo3);
 }
 
 template <int KMAX>
@@ -274,12 +284,15 @@ int launch_density(Context &c, const plan_params &p, uint32_t k, cudaStream_t s)
     uint32_t *redo = c.scratch.get<uint32_t>(n + 1), *nredo = c.scratch.get<uint32_t>(4);
     if (!redo || !nredo) return kErrOutOfMemory;
     PLAN_CUDA(cudaMemsetAsync(nredo, 0, 4, s));
+    const bool spl = !c.fs.median_kernel;
+    const SplineCells sc = c.fs.spline;
     rc = launch_by_cap(k, [&](auto capc) {
         constexpr int CAP = decltype(capc)::value;
         size_t sm = (size_t)CAP * 128 * 8;
-        if (sm > 48 * 1024) PLAN_CUDA(cudaFuncSetAttribute(k_density_f<CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        auto kern = spl ? k_density_f<CAP, 1> : k_density_f<CAP, 0>;
+        if (sm > 48 * 1024) PLAN_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         PLAN_CUDA(cudaEventRecord(c.kev[0], s));
-        k_density_f<CAP><<<grid_for(n, 128), 128, sm, s>>>(t, f, n, k, fpo3, c.tree.dens, redo, nredo, c.d_err);
+        kern<<<grid_for(n, 128), 128, sm, s>>>(t, f, n, k, fpo3, sc, c.tree.dens, redo, nredo, c.d_err);
         PLAN_CUDA(cudaEventRecord(c.kev[1], s));
         c.launches++;
         PLAN_CUDA(cudaGetLastError());
@@ -297,7 +310,8 @@ int launch_density(Context &c, const plan_params &p, uint32_t k, cudaStream_t s)
     return launch_by_k(k, [&](auto km, int threads) {
         constexpr int KM = decltype(km)::value;
         size_t sm = (size_t)KM * threads * 12;
-        k_density_list<KM><<<grid_for(h, threads), threads, sm, s>>>(t, redo, h, k, fpo3, c.tree.dens, c.d_err);
+        auto kern = spl ? k_density_list<KM, 1> : k_density_list<KM, 0>;
+        kern<<<grid_for(h, threads), threads, sm, s>>>(t, redo, h, k, fpo3, sc, c.tree.dens, c.d_err);
         c.launches++;
         PLAN_CUDA(cudaGetLastError());
         return (int)kOk;
@@ -350,7 +364,8 @@ int launch_density_at(Context &c, const double *d_q3, const double *d_est, uint3
     return launch_by_k(k, [&](auto km, int threads) {
         constexpr int KM = decltype(km)::value;
         size_t sm = (size_t)KM * threads * 12;
-        k_density_at<KM><<<grid_for(nq, threads), threads, sm, s>>>(t, d_q3, d_est, nq, k, fpo3, d_out, c.d_err);
+        auto kern = c.fs.median_kernel ? k_density_at<KM, 0> : k_density_at<KM, 1>;
+        kern<<<grid_for(nq, threads), threads, sm, s>>>(t, d_q3, d_est, nq, k, fpo3, c.fs.spline, d_out, c.d_err);
         c.launches++;
         PLAN_CUDA(cudaGetLastError());
         return (int)kOk;

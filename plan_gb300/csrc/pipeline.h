@@ -20,6 +20,7 @@
 
 #include "common.cuh"
 #include "plan_gpu.h"
+#include "spline.cuh"
 
 namespace plan {
 
@@ -65,7 +66,8 @@ struct FindScalars {
     double density_threshold, peak_density_threshold, clump_mass_threshold;
     double clump_diffuse_threshold, Hill_fraction_for_merge;
     uint32_t knn, hop;
-    int median_kernel;
+    int median_kernel;    // 0: the spline kernel (fewer than 4 particles per horizontal cell)
+    SplineCells spline;   // its cell constants
 };
 
 struct Context {

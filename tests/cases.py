@@ -54,7 +54,13 @@ CASES = [
     Case("w2_250k", 2, 250000, 3, 64),
     Case("config1_262k", 1, 262144, 1, 128),
 ]
-BY_NAME = {c.name: c for c in CASES}
+# fewer than four particles per horizontal grid cell (N < 4 Nx Ny): the spline density kernel
+# and the small-mass / low-peak pruning right after HOP
+SPLINE = [
+    Case("w1_50k_spline", 1, 50000, 31, 128),
+    Case("w1_20k_spline80", 1, 20000, 35, 80),
+]
+BY_NAME = {c.name: c for c in CASES + SPLINE}
 # command-line and parameter variants of one snapshot: (name, case, extra arguments)
 VARIANTS = [
     ("w1_20k_parlist_s3", Case("w1_20k", 1, 20000, 5, 32), ["--Save_Clumps", "-s", "3"]),

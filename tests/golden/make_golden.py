@@ -176,7 +176,7 @@ def main() -> None:
         multi_snapshot()
     if not only or "variants" in only:
         variants()
-    for c in cases.CASES:
+    for c in cases.CASES + cases.SPLINE:
         if only and c.name not in only:
             continue
         with tempfile.TemporaryDirectory() as tmp:

@@ -14,7 +14,7 @@ import pytest
 import cases
 from conftest import GOLDEN, golden
 
-CPU_CASES = [c.name for c in cases.CASES]
+CPU_CASES = [c.name for c in cases.CASES + cases.SPLINE]
 
 
 @pytest.fixture(scope="module")
