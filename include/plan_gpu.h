@@ -61,6 +61,8 @@ typedef struct plan_params {
     int32_t box_set;                /* box and masses taken from a first snapshot */
     /* command-line flags */
     int32_t no_ghost;               /* --No_Ghost */
+    int32_t user_box;               /* -x/-y/-z given (src/global.cpp:398-440) */
+    double user_box_min[3], user_box_max[3]; /* their limits, lo <= hi; 0,0 on an axis = the box's extent */
 } plan_params;
 
 /* Defaults of NumericalParameters (src/global.hpp:686-862). */

@@ -54,6 +54,7 @@ def lib() -> C.CDLL:
         L.orc_clumps.argtypes = [vp, C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_write_outputs.argtypes = [vp, C.c_char_p, C.c_int]
         L.orc_morton_order.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p]
+        L.orc_set_user_box.argtypes = [vp, C.c_void_p, C.c_void_p]
         _lib = L
     return _lib
 
@@ -69,12 +70,17 @@ def morton_order(keys3: np.ndarray) -> np.ndarray:
 class Oracle:
     """One snapshot through the CPU restatement: tree, densities, HOP, clumps."""
 
-    def __init__(self, lis, param: str | None, threads: int = 0, pow_mode: int = 0, no_ghost: bool = False):
-        """lis: one path or the list of files of one snapshot (id0 first)."""
+    def __init__(self, lis, param: str | None, threads: int = 0, pow_mode: int = 0, no_ghost: bool = False, user_box=None):
+        """lis: one path or the list of files of one snapshot (id0 first); user_box: optional
+        ((lo_x, lo_y, lo_z), (hi_x, hi_y, hi_z)) as given by -x/-y/-z (0, 0 = unrestricted)."""
         L = lib()
         self._h = L.orc_open((param or "").encode(), int(threads), int(pow_mode), int(no_ghost))
         if not self._h:
             raise RuntimeError(f"oracle: cannot read parameters {param}")
+        if user_box is not None:
+            lo = np.ascontiguousarray(user_box[0], dtype=np.float64)
+            hi = np.ascontiguousarray(user_box[1], dtype=np.float64)
+            L.orc_set_user_box(self._h, lo.ctypes.data, hi.ctypes.data)
         paths = [lis] if isinstance(lis, (str, bytes)) or not hasattr(lis, "__iter__") else list(lis)
         rc = L.orc_load(self._h, "\n".join(str(p) for p in paths).encode())
         if rc:

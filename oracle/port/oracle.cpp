@@ -211,6 +211,26 @@ void finish_read(Snapshot &s, Params &p, bool first_file) {  // src/tree.hpp:155
             p.mass_per_particle[i] = p.mass_fraction_per_species[i] * p.mass_total_code_units / s.num_particles;
         }
     }
+    if (p.user_box) {  // src/tree.hpp:1585-1620
+        auto in_range = [&](const V3 &v) {
+            bool in = true;
+            for (int d = 0; d < 3; ++d) in = in && (v[d] >= p.user_box_min[d] && v[d] <= p.user_box_max[d]);
+            return in;
+        };
+        for (int d = 0; d < 3; ++d) {
+            if (p.user_box_min[d] == 0 && p.user_box_max[d] == 0) {
+                p.user_box_min[d] = p.box_min[d];
+                p.user_box_max[d] = p.box_max[d];
+            }
+        }
+        if (!(in_range(p.box_min) && in_range(p.box_max))) {
+            std::vector<Particle> kept;
+            for (uint32_t i = 0; i < s.num_particles; ++i)
+                if (in_range(s.parts[i].pos)) kept.push_back(s.parts[i]);
+            s.parts.swap(kept);
+            s.num_particles = (uint32_t)s.parts.size();
+        }
+    }
 }
 
 void make_ghosts(Snapshot &s, const Params &p) {  // src/tree.hpp:1626-1754

@@ -76,6 +76,10 @@ struct Params {
     unsigned num_peaks = 0;
     double clump_diffuse_threshold = -1.0, Hill_fraction_for_merge = -1.0;
     double min_trusted_mass = 2.87621e-6;
+    // -x/-y/-z user box (progIO->user_box_min/max and flags.user_defined_box_flag,
+    // src/global.cpp:398-440)
+    bool user_box = false;
+    V3 user_box_min{0, 0, 0}, user_box_max{0, 0, 0};
 
     void derive();  // CalculateNewParameters, src/global.cpp:28-47
 };

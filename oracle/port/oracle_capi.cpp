@@ -41,6 +41,16 @@ void *orc_open(const char *param_path, int threads, int pow_mode, int no_ghost) 
 
 void orc_close(void *h) { delete static_cast<Ctx *>(h); }
 
+// -x/-y/-z user box for the next orc_load (lo <= hi per axis; 0,0 = the box's extent)
+void orc_set_user_box(void *h, const double *lo3, const double *hi3) {
+    Ctx *c = static_cast<Ctx *>(h);
+    c->par.user_box = true;
+    for (int d = 0; d < 3; ++d) {
+        c->par.user_box_min[d] = lo3[d];
+        c->par.user_box_max[d] = hi3[d];
+    }
+}
+
 // Read one combined .lis file (first file of a run), make ghosts and build the tree.
 // lis_paths: one path, or the files of one snapshot separated by newlines (id0 first)
 int orc_load(void *h, const char *lis_paths) {

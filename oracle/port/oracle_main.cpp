@@ -9,6 +9,7 @@
 #include <iomanip>
 #include <sstream>
 #include <string>
+#include <utility>
 #include <vector>
 
 #ifdef _OPENMP
@@ -39,6 +40,8 @@ int main(int argc, char **argv) {
     int num_cpus = 1, start = 0, end = 0, step = 1, pow_mode = 0, threads = 0;
     unsigned sampling = 1;
     std::string dir, base, post, out, param;
+    bool user_box = false;
+    double box_lo[3] = {0, 0, 0}, box_hi[3] = {0, 0, 0};
     int o, idx;
     while ((o = getopt_long(argc, argv, ":c:i:b:p:f:o:t:s:x:y:z:hP:T:", opts, &idx)) != -1) {
         switch (o) {
@@ -69,7 +72,15 @@ int main(int argc, char **argv) {
         case 'P': pow_mode = std::atoi(optarg); break;
         case 'T': threads = std::atoi(optarg); break;
         case 'h': f_help = 1; break;
-        case 'x': case 'y': case 'z': break;  // user box: not used by the oracle's tests
+        case 'x': case 'y': case 'z': {  // src/global.cpp:398-440
+            const int d = o == 'x' ? 0 : o == 'y' ? 1 : 2;
+            std::istringstream is(optarg);
+            char sep;
+            is >> box_lo[d] >> sep >> box_hi[d];
+            if (box_lo[d] > box_hi[d]) std::swap(box_lo[d], box_hi[d]);
+            user_box = true;
+            break;
+        }
         default: std::fprintf(stderr, "Error: Unknown/invalid option\n"); return 2;
         }
     }
@@ -77,6 +88,11 @@ int main(int argc, char **argv) {
     if (!dir.empty() && dir.back() != '/') dir.push_back('/');
     Params par;
     if (!param.empty()) { int rc = read_param_file(param, par); if (rc) return rc; }
+    par.user_box = user_box;
+    for (int d = 0; d < 3; ++d) {
+        par.user_box_min[d] = box_lo[d];
+        par.user_box_max[d] = box_hi[d];
+    }
     int nthreads = threads > 0 ? threads : (int)par.num_threads;
 #ifdef _OPENMP
     if (nthreads <= 0) nthreads = omp_get_max_threads();

@@ -52,7 +52,8 @@ class Params(C.Structure):
         ("mass_total_code_units", C.c_double), ("G_tilde", C.c_double), ("mass_physical", C.c_double),
         ("grav_constant", C.c_double), ("shear_speed", C.c_double), ("min_trusted_mass", C.c_double),
         ("ntypes", C.c_uint32), ("mass_per_particle", C.c_double * 16), ("mass_fraction_per_species", C.c_double * 16),
-        ("box_set", C.c_int32), ("no_ghost", C.c_int32),
+        ("box_set", C.c_int32), ("no_ghost", C.c_int32), ("user_box", C.c_int32), ("user_box_min", C.c_double * 3),
+        ("user_box_max", C.c_double * 3),
     ]
 
 

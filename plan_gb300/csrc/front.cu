@@ -64,6 +64,39 @@ __global__ void k_gather_in(const uint32_t *perm, size_t n, const double4_32a *p
     type2[i] = type[s];
 }
 
+// ---------------------------------------------------------------- user box (src/tree.hpp:1585-1620)
+struct UserBox {
+    double lo[3], hi[3];
+};
+
+// 1 for particles (in (cpu_id, id_in_run) order) inside the closed user box (SmallVec::InRange,
+// src/global.hpp:543-549)
+__global__ void k_box_flags(const uint32_t *order, uint32_t n, const double4_32a *pos, UserBox b, uint32_t *flag) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double4_32a p = pos[order[i]];
+    const bool in = p.x >= b.lo[0] && p.x <= b.hi[0] && p.y >= b.lo[1] && p.y <= b.hi[1] && p.z >= b.lo[2] && p.z <= b.hi[2];
+    flag[i] = in ? 1u : 0u;
+}
+
+// stable compaction of the kept particles: their file-order index and their rank before the
+// selection (the particle id, assigned before the box is applied)
+__global__ void k_box_compact(const uint32_t *order, uint32_t n, const uint32_t *flag, const uint32_t *off, uint32_t *src, uint32_t *rank) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || !flag[i]) return;
+    src[off[i]] = order[i];
+    rank[off[i]] = i;
+}
+
+// particle ids of the tree points: kept originals take their rank before the selection, ghosts
+// keep theirs (numbered from the kept count, src/tree.hpp:1633)
+__global__ void k_box_ids(uint32_t *orig, uint32_t n, uint32_t nkept, const uint32_t *rank) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const uint32_t o = orig[t];
+    if (o < nkept) orig[t] = rank[o];
+}
+
 // ---------------------------------------------------------------- ghosts
 struct GhostGeom {
     double lo[3], hi[3];      // non-ghost region
@@ -588,7 +621,7 @@ int build_tree(Context &c, const plan_lis_view &v, plan_params &p, int first_fil
     uint64_t N64 = 0;
     for (uint32_t b = 0; b < v.nblocks; ++b) N64 += v.counts[b];
     if (N64 == 0 || N64 >= 0xfffffff0ull) return kErrUnsupported;
-    const uint32_t N = (uint32_t)N64;
+    uint32_t N = (uint32_t)N64;  // the particles that take part (after the user box)
     c.n_input = N;
     c.time = v.time;
     // phase A (scratch arena): raw records and the unpacked particles in file order
@@ -602,6 +635,12 @@ int build_tree(Context &c, const plan_lis_view &v, plan_params &p, int first_fil
     unsigned long long *d_desc = S.get<unsigned long long>(4);
     size_t sortA = radix_sort96_scratch_bytes(N);
     void *scrA = S.take(sortA);
+    uint32_t *sel_src = nullptr, *sel_rank = nullptr, *sel_tot = nullptr;
+    if (p.user_box) {
+        sel_src = S.get<uint32_t>(N);
+        sel_rank = S.get<uint32_t>(N);
+        sel_tot = S.get<uint32_t>(4);
+    }
     if (S.failed) return kErrOutOfMemory;
 
     // 1. upload and unpack; a single block already in device memory is read in place
@@ -653,6 +692,44 @@ int build_tree(Context &c, const plan_lis_view &v, plan_params &p, int first_fil
         }
         p.box_set = 1;
     }
+    // user box (src/tree.hpp:1585-1620): an axis given as 0,0 takes the box's extent; a box
+    // that holds the whole domain changes nothing; otherwise only the particles inside it
+    // take part, keeping their ids and order
+    const uint32_t *gather_from = aidx;
+    bool selected = false;
+    if (p.user_box) {
+        UserBox ub;
+        bool covers = true;
+        for (int d = 0; d < 3; ++d) {
+            if (p.user_box_min[d] == 0 && p.user_box_max[d] == 0) {
+                p.user_box_min[d] = p.box_min[d];
+                p.user_box_max[d] = p.box_max[d];
+            }
+            ub.lo[d] = p.user_box_min[d];
+            ub.hi[d] = p.user_box_max[d];
+        }
+        for (int d = 0; d < 3; ++d)
+            covers = covers && p.box_min[d] >= ub.lo[d] && p.box_min[d] <= ub.hi[d] && p.box_max[d] >= ub.lo[d] && p.box_max[d] <= ub.hi[d];
+        if (!covers) {
+            // aw0/aw1 (the sort keys) are free after the sort; the sort scratch serves the scan
+            k_box_flags<<<grid_for(N, 256), 256, 0, s>>>(aidx, N, tmp_pos, ub, aw0);
+            int rc = scan_u32(aw0, aw1, N, sel_tot, scrA, sortA, s);
+            if (rc) return rc;
+            k_box_compact<<<grid_for(N, 256), 256, 0, s>>>(aidx, N, aw0, aw1, sel_src, sel_rank);
+            c.launches += 2;
+            uint32_t kept = 0;
+            PLAN_CUDA(cudaMemcpyAsync(&kept, sel_tot, 4, cudaMemcpyDeviceToHost, s));
+            PLAN_CUDA(cudaStreamSynchronize(s));
+            if (kept == 0) {
+                c.last_error = "no particle lies inside the user box (-x/-y/-z)";
+                return kErrUnsupported;
+            }
+            N = kept;
+            c.n_input = N;
+            gather_from = sel_src;
+            selected = true;
+        }
+    }
     GhostGeom g;
     for (int d = 0; d < 3; ++d) {
         double w = p.box_half_width[d] - p.ghost_zone_width[d];
@@ -667,7 +744,8 @@ int build_tree(Context &c, const plan_lis_view &v, plan_params &p, int first_fil
     g.shear_dt = p.shear_speed * v.time;
     uint64_t G = 0;
     if (!p.no_ghost) {
-        k_ghost_total<<<grid_for(N, 256), 256, 0, s>>>(tmp_pos, N, g, d_desc + 2);
+        // over every particle of the file: an upper bound when a user box keeps fewer
+        k_ghost_total<<<grid_for((uint32_t)N64, 256), 256, 0, s>>>(tmp_pos, (uint32_t)N64, g, d_desc + 2);
         PLAN_CUDA(cudaMemcpyAsync(&G, d_desc + 2, 8, cudaMemcpyDeviceToHost, s));
         PLAN_CUDA(cudaStreamSynchronize(s));
         c.launches++;
@@ -676,7 +754,7 @@ int build_tree(Context &c, const plan_lis_view &v, plan_params &p, int first_fil
     if (Tmax >= 0xfffffff0ull) return kErrUnsupported;
     // phase B (snapshot arena): everything the later stages keep, sized by the exact count
     {
-        int erc = c.ensure(c.arena, (size_t)Tmax * kArenaBytesPerTreePoint + (64u << 20));
+        int erc = c.ensure(c.arena, (size_t)Tmax * kArenaBytesPerTreePoint + (64u << 20) + (selected ? (size_t)N * 4 : 0));
         if (erc) return erc;
     }
     c.arena.used = 0;
@@ -687,9 +765,11 @@ int build_tree(Context &c, const plan_lis_view &v, plan_params &p, int first_fil
     uint32_t *kw0 = A.get<uint32_t>(Tmax), *kw1 = A.get<uint32_t>(Tmax), *kw2 = A.get<uint32_t>(Tmax), *kidx = A.get<uint32_t>(Tmax);
     uint32_t *d_u32 = A.get<uint32_t>(Tmax + 1);   // counts / offsets
     uint32_t *d_tot = A.get<uint32_t>(4);
+    uint32_t *keep_rank = selected ? A.get<uint32_t>(N) : nullptr;  // ids of the kept particles
     if (A.failed) return kErrOutOfMemory;
-    k_gather_in<<<grid_for(N, 256), 256, 0, s>>>(aidx, N, tmp_pos, tmp_vel, tmp_type, in_pos, in_vel, in_type);
+    k_gather_in<<<grid_for(N, 256), 256, 0, s>>>(gather_from, N, tmp_pos, tmp_vel, tmp_type, in_pos, in_vel, in_type);
     c.launches++;
+    if (selected) PLAN_CUDA(cudaMemcpyAsync(keep_rank, sel_rank, (size_t)N * 4, cudaMemcpyDeviceToDevice, s));
     cudaEventRecord(ev[1], s);
     // phase A buffers are dead from here on: the scratch arena is reused
     PLAN_CUDA(cudaStreamSynchronize(s));
@@ -773,6 +853,10 @@ int build_tree(Context &c, const plan_lis_view &v, plan_params &p, int first_fil
         for (int t = 0; t < 16; ++t) mt.m[t] = p.mass_per_particle[t];
         int rc = build_octree(c, in_pos, in_vel, in_type, T, box, mt.m, mt.ntypes, c.tree, s, ev[3]);
         if (rc) return rc;
+    }
+    if (selected) {
+        k_box_ids<<<grid_for(c.tree.Tu, 256), 256, 0, s>>>(c.tree.orig, c.tree.Tu, N, keep_rank);
+        c.launches++;
     }
     cudaEventRecord(ev[4], s);
     PLAN_CUDA(cudaStreamSynchronize(s));

@@ -3,8 +3,9 @@
 // Same command line (src/global.cpp:247-289, usage 558-578), same file names
 // (src/global.cpp:620-675) and the same outputs: <out-stem>_planetesimals.txt
 // (WriteBasicResults), peaks_at_<time>.txt and, with --Save_Clumps, ParList.<NNNN>/.
-// Grid analyses (--Basic_Analyses, --Density_Vs_Scale, --Temp_Calculation) are not part
-// of this build and are rejected with exit code 2.
+// -x/-y/-z user boxes restrict the particles read, as in the reference. Grid analyses
+// (--Basic_Analyses, --Density_Vs_Scale, --Temp_Calculation) are not part of this build and
+// are rejected with exit code 2.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -14,6 +15,7 @@
 #include <iostream>
 #include <sstream>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "plan_gpu.h"
@@ -81,6 +83,7 @@ int main(int argc, char **argv) {
     unsigned sampling = 1;
     std::string dir, base, post, out, param;
     bool user_box = false;
+    double box_lo[3] = {0, 0, 0}, box_hi[3] = {0, 0, 0};  // user box, 0,0 = not restricted on that axis
     if (argc < 13) {
         usage(argv[0]);
         return 0;
@@ -129,7 +132,15 @@ int main(int argc, char **argv) {
             }
             break;
         }
-        case 'x': case 'y': case 'z': user_box = true; break;
+        case 'x': case 'y': case 'z': {  // src/global.cpp:398-440
+            const int d = o == 'x' ? 0 : o == 'y' ? 1 : 2;
+            std::istringstream is(optarg);
+            char sep;
+            is >> box_lo[d] >> sep >> box_hi[d];
+            if (box_lo[d] > box_hi[d]) std::swap(box_lo[d], box_hi[d]);
+            user_box = true;
+            break;
+        }
         case 'h': f_help = 1; break;
         case ':':
             std::cerr << "Error: Option -" << optopt << " requires an arugment.\n";
@@ -155,14 +166,15 @@ int main(int argc, char **argv) {
         std::cerr << "Error: only --Find_Clumps is available in this build (grid analyses are not part of it)." << std::endl;
         return 2;
     }
-    if (user_box) {
-        std::cerr << "Error: -x/-y/-z user boxes are not available in this build yet." << std::endl;
-        return 2;
-    }
     if (dir.empty() || *dir.rbegin() != '/') dir.push_back('/');
     plan_params par;
     plan_params_init(&par);
     par.no_ghost = f_noghost;
+    par.user_box = user_box ? 1 : 0;
+    for (int d = 0; d < 3; ++d) {
+        par.user_box_min[d] = box_lo[d];
+        par.user_box_max[d] = box_hi[d];
+    }
     if (!param.empty()) {
         int rc = plan_params_read(param.c_str(), &par);
         if (rc) return exit_code(rc);

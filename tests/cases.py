@@ -68,6 +68,12 @@ VARIANTS = [
     ("w1_20k_no_ghost", Case("w1_20k", 1, 20000, 5, 32), ["--No_Ghost", "--Save_Clumps"]),
     ("w1_20k_diffuse_hill", Case("w1_20k_dh", 1, 20000, 5, 32, extra={"clump_diffuse_threshold": 0.45, "Hill_fraction_for_merge": 0.4}),
      ["--Save_Clumps"]),
+    # user boxes (-x/-y/-z): only the particles inside take part, with their ids; limits given
+    # high before low are swapped; a box holding the whole domain changes nothing
+    ("w1_20k_box_x", Case("w1_20k", 1, 20000, 5, 32), ["-x", "-0.06,0.07", "--Save_Clumps"]),
+    ("w1_20k_box_yz", Case("w1_20k_border", 1, 20000, 9, 32, edit="border"),
+     ["-y", "0.09,-0.06", "-z", "-0.06,0.05", "--No_Ghost", "--Save_Clumps"]),
+    ("w1_20k_box_all", Case("w1_20k", 1, 20000, 5, 32), ["-x", "-0.2,0.2"]),
 ]
 # one run over two snapshot files (-f 0:1): the second is later in time and uses the first's box
 MULTI = [Case("multi_0", 1, 20000, 5, 32), Case("multi_1", 1, 20000, 6, 32, time=0.25)]

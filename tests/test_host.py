@@ -54,6 +54,28 @@ def test_nm_shows_only_c_symbols(built):
     assert not [s for s in exported if s.startswith("_Z") and "plan_" in s and "plan_" == s[:5]]
 
 
+def test_struct_layouts_match_the_header(built, tmp_path):
+    """The ctypes mirrors of the ABI structs have the C sizes and field offsets."""
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    fields = {"plan_params": (built.Params, [f[0] for f in built.Params._fields_]),
+              "plan_lis_view": (built.LisView, [f[0] for f in built.LisView._fields_]),
+              "plan_clump_info": (built.ClumpInfo, [f[0] for f in built.ClumpInfo._fields_])}
+    src = ["#include <cstddef>", "#include <cstdio>", '#include "plan_gpu.h"', "int main() {"]
+    for st, (_, names) in fields.items():
+        src.append(f'    std::printf("{st} %zu\\n", sizeof({st}));')
+        for n in names:
+            src.append(f'    std::printf("{st}.{n} %zu\\n", offsetof({st}, {n}));')
+    src.append("}")
+    (tmp_path / "l.cpp").write_text("\n".join(src) + "\n")
+    subprocess.run(["g++", "-I", str(ROOT / "include"), str(tmp_path / "l.cpp"), "-o", str(tmp_path / "l")], check=True)
+    got = dict(ln.split() for ln in subprocess.run([str(tmp_path / "l")], capture_output=True, text=True, check=True).stdout.splitlines())
+    for st, (cls, names) in fields.items():
+        assert int(got[st]) == C.sizeof(cls), st
+        for n in names:
+            assert int(got[f"{st}.{n}"]) == getattr(cls, n).offset, (st, n)
+
+
 # ---------------------------------------------------------------- parameters
 def test_params_defaults(built):
     p = built.params()
