@@ -30,6 +30,7 @@
 
 #include "catalogue.h"
 #include "hop.h"
+#include "lib_sort.cuh"
 #include "pipeline.h"
 #include "sort.h"
 #include "ordered_sum.cuh"
@@ -222,12 +223,13 @@ __global__ void k_dist(const uint32_t *list, CT ct, Pool P, const double4_32a *p
 }
 
 // in-block bitonic sort by (distance, previous position) for segments <= kSmallSort
-__global__ void __launch_bounds__(1024) k_sort_small(const uint32_t *list, CT ct, Pool P) {
+__global__ void __launch_bounds__(1024) k_sort_small(const uint32_t *list, CT ct, Pool P, uint8_t *tie_flag) {
     __shared__ unsigned long long sk[kSmallSort];
     __shared__ uint32_t si[kSmallSort];
     __shared__ uint16_t sp[kSmallSort];
     uint32_t s = list[blockIdx.x];
     const uint32_t o = ct.moff[s], m = ct.mn[s];
+    if (threadIdx.x == 0) tie_flag[s] = 0;
     if (m > kSmallSort || m < 2) return;
     uint32_t n2 = 1;
     while (n2 < m) n2 <<= 1;
@@ -260,10 +262,29 @@ __global__ void __launch_bounds__(1024) k_sort_small(const uint32_t *list, CT ct
             __syncthreads();
         }
     }
+    // two members at exactly the same distance in a segment longer than the library's
+    // insertion-sort threshold: the pool keeps the sequence before the sort for k_lib_order
+    int tie = 0;
+    if (m > 16)
+        for (uint32_t k = threadIdx.x + 1; k < m; k += blockDim.x) tie |= sk[k] == sk[k - 1];
+    if (__syncthreads_or(tie)) {
+        if (threadIdx.x == 0) tie_flag[s] = 1;
+        return;
+    }
     for (uint32_t k = threadIdx.x; k < m; k += blockDim.x) {
         P.idx[o + k] = si[k];
         P.dist[o + k] = __longlong_as_double((long long)sk[k]);
     }
+}
+
+// segments whose sort met a tie: the reference's std::sort order (lib_sort.cuh), one thread
+// per segment; rare (two members of one clump at exactly the same distance)
+__global__ void k_lib_order(const uint32_t *list, uint32_t n, CT ct, Pool P, const uint8_t *tie_flag) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const uint32_t s = list[t];
+    if (!tie_flag[s]) return;
+    lib_sort(P.dist + ct.moff[s], P.idx + ct.moff[s], ct.mn[s]);
 }
 
 // radii after a sort (src/tree.hpp:4461-4511)
@@ -356,11 +377,18 @@ __global__ void k_large_gather(const uint32_t *list, uint32_t nl, const uint32_t
 }
 
 __global__ void k_large_scatter(const uint32_t *list, uint32_t nl, const uint32_t *base, CT ct, Pool P, const uint32_t *w0,
-                                const uint32_t *w1, const uint32_t *pay) {
+                                const uint32_t *w1, const uint32_t *pay, uint8_t *tie_flag) {
     uint32_t t = blockIdx.x;
     if (t >= nl) return;
     uint32_t s = list[t];
     const uint32_t o = ct.moff[s], m = ct.mn[s], b = base[t];
+    // a tie at equal distances: the unsorted members stay for k_lib_order (as in k_sort_small)
+    int tie = 0;
+    for (uint32_t k = threadIdx.x + 1; k < m; k += blockDim.x) tie |= w0[b + k] == w0[b + k - 1] && w1[b + k] == w1[b + k - 1];
+    if (__syncthreads_or(tie)) {
+        if (threadIdx.x == 0) tie_flag[s] = 1;
+        return;
+    }
     for (uint32_t k = threadIdx.x; k < m; k += blockDim.x) {
         unsigned long long bits = ((unsigned long long)w1[b + k] << 32) | w0[b + k];
         P.dist[o + k] = __longlong_as_double((long long)bits);
@@ -1571,6 +1599,7 @@ struct Stage {
     uint32_t *d_list = nullptr;   // scratch slot list (capacity C)
     uint32_t *d_list2 = nullptr;
     uint8_t *d_flag8 = nullptr;
+    uint8_t *d_tie = nullptr;  // per slot: the last member sort met a tie (k_sort_small, k_lib_order)
     uint32_t *d_u = nullptr;      // small device counters
     const DevTree &tr;
 
@@ -1635,7 +1664,7 @@ struct Stage {
         for (uint32_t v : mn_list) mx = std::max(mx, v);
         const unsigned ny = std::min(64u, std::max(1u, (mx + 8191) / 8192));
         k_dist<<<dim3(n, ny), 256, 0, s>>>(d_list, ct, P, tr.pos);
-        k_sort_small<<<n, 1024, 0, s>>>(d_list, ct, P);
+        k_sort_small<<<n, 1024, 0, s>>>(d_list, ct, P, d_tie);
         c.launches += 2;
         // segments longer than the in-block sort go through the radix sort
         std::vector<uint32_t> large, base;
@@ -1655,7 +1684,7 @@ struct Stage {
             k_large_gather<<<(unsigned)large.size(), 256, 0, s>>>(dl, (uint32_t)large.size(), db, ct, P, w0, w1, w2, pay);
             rc = radix_sort96(w0, w1, w2, pay, tot, scr, sb, s);
             if (rc) { S.used = mark; return rc; }
-            k_large_scatter<<<(unsigned)large.size(), 256, 0, s>>>(dl, (uint32_t)large.size(), db, ct, P, w0, w1, pay);
+            k_large_scatter<<<(unsigned)large.size(), 256, 0, s>>>(dl, (uint32_t)large.size(), db, ct, P, w0, w1, pay, d_tie);
             c.launches += 2 + 36;
             PLAN_CUDA(cudaGetLastError());
             rc = sync();
@@ -1664,6 +1693,8 @@ struct Stage {
             rc = up_list(list, d_list);
             if (rc) return rc;
         }
+        k_lib_order<<<(n + 63) / 64, 64, 0, s>>>(d_list, n, ct, P, d_tie);
+        c.launches++;
         if (radii) {
             k_one10th<<<n, 256, 0, s>>>(d_list, ct, P, tr.pos, tr.dens);
             c.launches++;
@@ -1861,6 +1892,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
     st.d_list = A.get<uint32_t>(C + 1);
     st.d_list2 = A.get<uint32_t>(C + 1);
     st.d_flag8 = A.get<uint8_t>(C + 1);
+    st.d_tie = A.get<uint8_t>(C + 1);
     st.d_u = A.get<uint32_t>(64);
     uint8_t *in_clump = A.get<uint8_t>(Tu);
     if (A.failed) return kErrOutOfMemory;
