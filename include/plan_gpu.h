@@ -136,6 +136,11 @@ const char *plan_catalogue_summary(const plan_catalogue *cat);
  * next to out_path; with save_clumps also ParList.<NNNN>/<peak_id>.txt
  * (src/tree.hpp:5191-5222), NNNN = file_number, every `sampling`-th member. */
 int plan_catalogue_write_peaks(const plan_catalogue *cat, const char *out_path, int save_clumps, int file_number, uint32_t sampling);
+/* OutputSinglePlanetesimal (src/tree.hpp:5191-5222) for every clump of a catalogue, with
+ * the lines formatted on the context's device: ParList.<NNNN>/<peak_id>.txt in the working
+ * directory, byte-identical to the member lists plan_catalogue_write_peaks writes with
+ * save_clumps (which formats them on the host). NNNN = file_number, every `sampling`-th member. */
+int plan_catalogue_write_parlists(plan_ctx *ctx, const plan_catalogue *cat, int file_number, uint32_t sampling);
 /* PlanetesimalList::WriteBasicResults (src/tree.hpp:4935-4953): the line for this snapshot
  * (with the header first when with_header != 0) into buf; returns the length or -1. */
 int plan_catalogue_basic_results(const plan_catalogue *cat, const plan_params *p, int with_header, char *buf, size_t cap);

@@ -109,6 +109,7 @@ def lib() -> C.CDLL:
             "plan_catalogue_get": (i32, [vp, u32, C.POINTER(ClumpInfo)]),
             "plan_catalogue_summary": (C.c_char_p, [vp]),
             "plan_catalogue_write_peaks": (i32, [vp, C.c_char_p, i32, i32, u32]),
+            "plan_catalogue_write_parlists": (i32, [vp, vp, i32, u32]),
             "plan_catalogue_basic_results": (i32, [vp, C.POINTER(Params), i32, C.c_char_p, C.c_size_t]),
             "plan_stage_count": (u64, [vp, i32]),
             "plan_stage_copy": (i32, [vp, i32, vp, C.c_size_t]),
@@ -135,7 +136,8 @@ EXPORTED = [
     "plan_params_init", "plan_params_read", "plan_params_derive", "plan_lis_read", "plan_lis_free", "plan_lis_count",
     "plan_lis_time", "plan_lis_get_view", "plan_ctx_create", "plan_ctx_destroy", "plan_last_error", "plan_footprint_bytes",
     "plan_build_tree", "plan_find_planetesimals", "plan_find_clumps", "plan_catalogue_free", "plan_catalogue_count",
-    "plan_catalogue_get", "plan_catalogue_summary", "plan_catalogue_write_peaks", "plan_catalogue_basic_results",
+    "plan_catalogue_get", "plan_catalogue_summary", "plan_catalogue_write_peaks", "plan_catalogue_write_parlists",
+    "plan_catalogue_basic_results",
     "plan_stage_count", "plan_stage_copy", "plan_knn", "plan_morton_order", "plan_morton_order_noalloc", "plan_stage_times", "plan_kernel_launches", "plan_counters",
     "plan_synth_default_spec", "plan_synth_records", "plan_synth_write_lis", "plan_synth_four_pi_G_for_mean",
 ]
@@ -323,6 +325,13 @@ class Finder:
         if rc:
             raise PlanError(rc, self.error())
         return out
+
+    def write_parlists(self, cat: "Catalogue", file_number: int = 0, sampling: int = 1) -> None:
+        """The --Save_Clumps member lists of cat (ParList.<NNNN>/ in the working directory),
+        formatted on this context's device."""
+        rc = lib().plan_catalogue_write_parlists(self._h, cat._h, int(file_number), int(sampling))
+        if rc:
+            raise PlanError(rc, self.error())
 
     def morton_order_noalloc(self, keys3: np.ndarray) -> np.ndarray:
         """morton_order without device allocation (at most PLAN_NOALLOC_SORT_MAX keys)."""

@@ -350,6 +350,16 @@ int plan_morton_order_noalloc(plan_ctx *h, const uint32_t *keys3, uint32_t n, ui
     return c.status_from(rc, "plan_morton_order_noalloc");
 }
 
+int plan_catalogue_write_parlists(plan_ctx *h, const plan_catalogue *cat, int file_number, uint32_t sampling) {
+    if (!h || !cat) return kErrArgument;
+    Context &c = h->c;
+    g_ctx = &c;
+    c.last_error.clear();
+    cudaSetDevice(c.device);
+    int rc = write_parlists_device(c, *cat, file_number, sampling, c.stream);
+    return c.status_from(rc, "plan_catalogue_write_parlists");
+}
+
 int plan_stage_times(const plan_ctx *h, double *ms, int n) {
     if (!h || !ms) return kErrArgument;
     for (int i = 0; i < n && i < 32; ++i) ms[i] = h->c.stage_ms[i];

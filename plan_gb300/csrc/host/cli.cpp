@@ -192,6 +192,8 @@ int main(int argc, char **argv) {
         plan_ctx_destroy(ctx);
         return 3;
     }
+    const char *pd_env = std::getenv("PLAN_PARLIST_DEVICE");
+    const bool parlist_device = pd_env && *pd_env == '1';
     std::ostringstream oc;  // keeps its formatting state across snapshots, as the reference's
     bool first = true;
     int status = 0;
@@ -238,7 +240,9 @@ int main(int argc, char **argv) {
         oc.str(std::string());
         oc.clear();
         oc << std::scientific;  // WriteBasicResults leaves the shared stream in scientific mode
-        rc = plan_catalogue_write_peaks(cat, out.c_str(), f_save, num, sampling);
+        // member lists formatted on the device with PLAN_PARLIST_DEVICE=1, else on the host
+        rc = plan_catalogue_write_peaks(cat, out.c_str(), f_save && !parlist_device, num, sampling);
+        if (!rc && f_save && parlist_device) rc = plan_catalogue_write_parlists(ctx, cat, num, sampling);
         if (rc) status = rc;
         char buf[1024];
         int len = plan_catalogue_basic_results(cat, &par, first ? 1 : 0, buf, sizeof(buf));

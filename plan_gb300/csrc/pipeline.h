@@ -104,6 +104,8 @@ int build_octree(Context &c, double4_32a *in_pos, double4_32a *in_vel, const uin
 TreeBox make_box(const double center[3], double half_width);
 // Stage 2: densities, densest neighbours, HOP groups, clump stage -> host catalogue.
 int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogue **out);
+// --Save_Clumps member lists of a catalogue, formatted on the device (parlist.cu).
+int write_parlists_device(Context &c, const plan_catalogue &cat, int file_number, uint32_t sampling, cudaStream_t s);
 // KNN queries at arbitrary positions on the current tree (inspection / tests).
 int knn_positions(Context &c, const double *pos3, uint32_t nq, uint32_t k, double est, uint32_t *idx, double *dr2);
 

@@ -3,17 +3,19 @@
 Each variant of tests/cases.py (sub-sampled member lists with -s, the num_peaks cap,
 --No_Ghost, the merge parameters, and -x/-y/-z user boxes) runs the plan_gpu binary with the
 reference's command line; its summary line, catalogue, basic-results file and every
---Save_Clumps member list must equal the reference's own files.
+--Save_Clumps member list must equal the reference's own files. The member lists formatted
+on the device (plan_catalogue_write_parlists) must equal the host-formatted ones.
 """
 from __future__ import annotations
 
 import json
+import os
 import subprocess
 
 import pytest
 
 import cases
-from conftest import GOLDEN, ROOT
+from conftest import GOLDEN, ROOT, golden
 
 pytestmark = pytest.mark.gpu
 
@@ -33,4 +35,48 @@ def test_cli_variants(name, case, extra, built, tmp_path):
     assert meta["summary"] in r.stdout
     assert (out / meta["peaks_file"]).read_bytes() == (g / meta["peaks_file"]).read_bytes()
     assert (out / "res_planetesimals.txt").read_bytes() == (g / "planetesimals.txt").read_bytes()
+    assert cases.parlist_digests(out) == meta["parlist"]
+
+
+@pytest.mark.parametrize("name,sampling", [("w1_20k", 1), ("w1_20k_sinks", 1), ("w1_20k", 3)])
+def test_device_member_lists(name, sampling, built, case_dir, tmp_path, monkeypatch):
+    """Member lists formatted on the device equal the host-formatted ones byte for byte (and
+    so the reference's): same files, same lines, every sub-sampling."""
+    m = case_dir(name)
+    p = built.params(m["param"])
+    snap = built.Snapshot(m["lis"])
+    f = built.Finder(0)
+    try:
+        cat = f.find_clumps(snap, p)
+        (tmp_path / "host").mkdir()
+        (tmp_path / "dev").mkdir()
+        monkeypatch.chdir(tmp_path / "host")
+        cat.write_peaks(str(tmp_path / "host" / "res.txt"), save_clumps=True, file_number=0, sampling=sampling)
+        monkeypatch.chdir(tmp_path / "dev")
+        f.write_parlists(cat, file_number=0, sampling=sampling)
+        host = sorted((tmp_path / "host" / "ParList.0000").iterdir())
+        dev = sorted((tmp_path / "dev" / "ParList.0000").iterdir())
+        assert [h.name for h in host] == [d.name for d in dev] and host
+        for h, d in zip(host, dev):
+            assert h.read_bytes() == d.read_bytes(), h.name
+        if sampling == 1:
+            assert cases.parlist_digests(tmp_path / "dev") == golden(name)["parlist"]
+        cat.close()
+    finally:
+        f.close()
+        snap.close()
+
+
+def test_cli_device_member_lists(built, tmp_path):
+    """The drop-in binary with PLAN_PARLIST_DEVICE=1 writes the reference's sub-sampled lists."""
+    name, case, extra = next(v for v in cases.VARIANTS if v[0] == "w1_20k_parlist_s3")
+    meta = json.loads((GOLDEN / name / "meta.json").read_text())
+    m = cases.materialise(case, tmp_path / "in")
+    out = tmp_path / "out"
+    out.mkdir()
+    cli = ROOT / "plan_gb300" / "lib" / "plan_gpu"
+    env = dict(os.environ, PLAN_PARLIST_DEVICE="1")
+    r = subprocess.run([str(cli)] + cases.cli_args(m, str(out / "res.txt")) + extra, cwd=out, capture_output=True, text=True,
+                       timeout=300, env=env)
+    assert r.returncode == 0, r.stderr
     assert cases.parlist_digests(out) == meta["parlist"]
