@@ -9,7 +9,8 @@
  * Conventions
  *   - Every call returns an int status: 0 ok, 2 argument, 3 I/O, 4 parameter, 5 CUDA,
  *     6 out of device memory / admission refused, 7 unsupported input, 8 device loop
- *     limit. The command-line front end maps 2/3/4 to the reference's exit codes.
+ *     limit, 9 pending (plan_poll: the request is queued or running). The command-line
+ *     front end maps 2/3/4 to the reference's exit codes.
  *   - Host buffers passed in are caller-owned and only read during the call. Device
  *     buffers are owned by the context and released by plan_ctx_destroy.
  *   - A context is bound to one device and is not thread-safe; use one per host thread.
@@ -27,8 +28,11 @@ extern "C" {
 
 #define PLAN_ABI_VERSION 1
 
+#define PLAN_PENDING 9
+
 typedef struct plan_ctx plan_ctx;
 typedef struct plan_lis plan_lis;
+typedef struct plan_server plan_server;
 typedef struct plan_catalogue plan_catalogue;
 
 /* NumericalParameters (src/global.hpp:676-874): the file-settable values, the reference's
@@ -98,6 +102,9 @@ int plan_lis_get_view(const plan_lis *lis, plan_lis_view *view);
 int plan_ctx_create(int device, plan_ctx **out);
 void plan_ctx_destroy(plan_ctx *ctx);
 const char *plan_last_error(const plan_ctx *ctx);
+/* Free the context's snapshot buffers (they grow back on the next snapshot); the stage
+ * arrays of the last snapshot are gone afterwards. New, for the serving loop's admission. */
+int plan_ctx_release(plan_ctx *ctx);
 /* Device bytes a snapshot of n particles needs (the serving admission estimate). */
 uint64_t plan_footprint_bytes(uint64_t n_particles, const plan_params *p);
 
@@ -144,6 +151,33 @@ int plan_catalogue_write_parlists(plan_ctx *ctx, const plan_catalogue *cat, int 
 /* PlanetesimalList::WriteBasicResults (src/tree.hpp:4935-4953): the line for this snapshot
  * (with the header first when with_header != 0) into buf; returns the length or -1. */
 int plan_catalogue_basic_results(const plan_catalogue *cat, const plan_params *p, int with_header, char *buf, size_t cap);
+
+/* ---------------------------------------------------------------- serving
+ * New, no counterpart in the reference (which processes its snapshot list one by one):
+ * snapshots submitted from any thread run concurrently on one device, each on one of
+ * `workers` contexts with its own stream and buffers. A request is admitted in arrival order
+ * when a worker is free and the device footprints (plan_footprint_bytes) of the running
+ * requests plus its own fit in `hbm_budget` bytes (0 = 90% of the device's free memory at
+ * creation); when the oldest waiting request does not fit, later ones that fit may start
+ * first, at most 2 x workers times before it. Workers keep their buffers between requests
+ * and give them back (plan_ctx_release) when a waiting request needs the room. Each request
+ * is computed exactly as plan_find_clumps computes it alone. */
+int plan_server_create(int device, int workers, uint64_t hbm_budget, plan_server **out);
+/* Waits for the running requests; queued ones are dropped. */
+void plan_server_destroy(plan_server *srv);
+/* Queue one snapshot (first_file as in plan_find_clumps; p is copied). The view's host
+ * records must stay valid until plan_poll has returned the request. Status 6 when the
+ * snapshot alone does not fit the budget. */
+int plan_submit(plan_server *srv, const plan_lis_view *snap, const plan_params *p, int first_file, uint64_t *request);
+/* The request's catalogue (caller frees) and its latency from submission to completion, in
+ * milliseconds: 0 when done, PLAN_PENDING while queued or running (wait = 0; wait != 0
+ * blocks until done), or the request's error status with its message in
+ * plan_server_error. A request is returned once. */
+int plan_poll(plan_server *srv, uint64_t request, int wait, plan_catalogue **out, double *latency_ms);
+/* Message of the last failed request returned by plan_poll on this server. */
+const char *plan_server_error(const plan_server *srv);
+/* Largest sum of worker holds seen against the budget, and how many holds were given back. */
+int plan_server_stats(const plan_server *srv, uint64_t *peak_held_bytes, uint64_t *releases);
 
 /* ---------------------------------------------------------------- inspection
  * Stage arrays of the last snapshot, for parity tests and profiling. */

@@ -110,6 +110,13 @@ def lib() -> C.CDLL:
             "plan_catalogue_summary": (C.c_char_p, [vp]),
             "plan_catalogue_write_peaks": (i32, [vp, C.c_char_p, i32, i32, u32]),
             "plan_catalogue_write_parlists": (i32, [vp, vp, i32, u32]),
+            "plan_ctx_release": (i32, [vp]),
+            "plan_server_create": (i32, [i32, i32, u64, C.POINTER(vp)]),
+            "plan_server_destroy": (None, [vp]),
+            "plan_submit": (i32, [vp, C.POINTER(LisView), C.POINTER(Params), i32, C.POINTER(C.c_uint64)]),
+            "plan_poll": (i32, [vp, u64, i32, C.POINTER(vp), C.POINTER(C.c_double)]),
+            "plan_server_error": (C.c_char_p, [vp]),
+            "plan_server_stats": (i32, [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
             "plan_catalogue_basic_results": (i32, [vp, C.POINTER(Params), i32, C.c_char_p, C.c_size_t]),
             "plan_stage_count": (u64, [vp, i32]),
             "plan_stage_copy": (i32, [vp, i32, vp, C.c_size_t]),
@@ -137,7 +144,8 @@ EXPORTED = [
     "plan_lis_time", "plan_lis_get_view", "plan_ctx_create", "plan_ctx_destroy", "plan_last_error", "plan_footprint_bytes",
     "plan_build_tree", "plan_find_planetesimals", "plan_find_clumps", "plan_catalogue_free", "plan_catalogue_count",
     "plan_catalogue_get", "plan_catalogue_summary", "plan_catalogue_write_peaks", "plan_catalogue_write_parlists",
-    "plan_catalogue_basic_results",
+    "plan_catalogue_basic_results", "plan_ctx_release", "plan_server_create", "plan_server_destroy", "plan_submit", "plan_poll",
+    "plan_server_error", "plan_server_stats",
     "plan_stage_count", "plan_stage_copy", "plan_knn", "plan_morton_order", "plan_morton_order_noalloc", "plan_stage_times", "plan_kernel_launches", "plan_counters",
     "plan_synth_default_spec", "plan_synth_records", "plan_synth_write_lis", "plan_synth_four_pi_G_for_mean",
 ]
@@ -358,6 +366,60 @@ class Finder:
     def close(self):
         if self._h:
             lib().plan_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+PLAN_PENDING = 9
+
+
+class Server:
+    """The serving loop (plan_server_*): snapshots submitted here run concurrently on one
+    device over `workers` contexts, admitted by device footprint against `hbm_budget` bytes
+    (0 = 90% of the free memory). Keep each Snapshot alive until its request is polled."""
+
+    def __init__(self, device: int = 0, workers: int = 2, hbm_budget: int = 0):
+        h = C.c_void_p()
+        rc = lib().plan_server_create(int(device), int(workers), int(hbm_budget), C.byref(h))
+        if rc:
+            raise PlanError(rc, "creating the serving loop")
+        self._h = h
+        self._params = {}  # request -> Params copy kept alive with the request
+
+    def submit(self, snap: Snapshot, p: Params, first_file: bool = True) -> int:
+        rid = C.c_uint64()
+        rc = lib().plan_submit(self._h, C.byref(snap.view), C.byref(p), int(first_file), C.byref(rid))
+        if rc:
+            raise PlanError(rc, self.error())
+        return int(rid.value)
+
+    def poll(self, request: int, wait: bool = False):
+        """(Catalogue, latency in ms) when done, None while queued or running."""
+        h = C.c_void_p()
+        lat = C.c_double()
+        rc = lib().plan_poll(self._h, int(request), int(wait), C.byref(h), C.byref(lat))
+        if rc == PLAN_PENDING:
+            return None
+        if rc:
+            raise PlanError(rc, self.error())
+        return Catalogue(h), float(lat.value)
+
+    def error(self) -> str:
+        return lib().plan_server_error(self._h).decode()
+
+    def stats(self) -> dict:
+        peak, rel = C.c_uint64(), C.c_uint64()
+        lib().plan_server_stats(self._h, C.byref(peak), C.byref(rel))
+        return {"peak_held_bytes": int(peak.value), "releases": int(rel.value)}
+
+    def close(self):
+        if self._h:
+            lib().plan_server_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -23,7 +23,7 @@ OUT = PKG / "lib"
 OBJ = PKG / "_build"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["radix_sort.cu", "scan.cu", "introsort.cu", "front.cu", "knn.cu", "hop.cu", "clumps.cu", "parlist.cu", "capi.cu"]
+CU_SOURCES = ["radix_sort.cu", "scan.cu", "introsort.cu", "front.cu", "knn.cu", "hop.cu", "clumps.cu", "parlist.cu", "server.cu", "capi.cu"]
 HOST_SOURCES = ["host/params.cpp", "host/lis.cpp", "host/catalogue.cpp", "host/synth.cpp"]
 
 
@@ -56,7 +56,8 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
     nvcc = str(cuda / "bin" / "nvcc")
     OUT.mkdir(exist_ok=True)
     OBJ.mkdir(exist_ok=True)
-    headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list((ROOT / "include").glob("*.h"))
+    headers = (list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list((CSRC / "host").glob("*.hpp")) +
+               list((ROOT / "include").glob("*.h")))
     inc = ["-I" + str(ROOT / "include"), "-I" + str(CSRC)]
     steps = []
     objs = []

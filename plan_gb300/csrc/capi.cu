@@ -110,6 +110,22 @@ void plan_ctx_destroy(plan_ctx *h) {
 
 const char *plan_last_error(const plan_ctx *h) { return h ? h->c.last_error.c_str() : "no context"; }
 
+int plan_ctx_release(plan_ctx *h) {
+    if (!h) return kErrArgument;
+    Context &c = h->c;
+    cudaSetDevice(c.device);
+    if (c.stream) cudaStreamSynchronize(c.stream);
+    for (Arena *a : {&c.arena, &c.scratch}) {
+        if (a->base) cudaFree(a->base);
+        a->base = nullptr;
+        a->cap = a->used = 0;
+        a->failed = false;
+    }
+    c.tree = DevTree{};
+    c.densest = c.peak = nullptr;
+    return kOk;
+}
+
 uint64_t plan_footprint_bytes(uint64_t n, const plan_params *) {
     uint64_t a, s;
     footprint(n, a, s);

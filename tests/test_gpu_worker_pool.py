@@ -1,0 +1,84 @@
+"""The serving loop on the GPU (needs a GB300): plan_submit / plan_poll.
+
+Snapshots of different sizes are submitted together from several threads and run
+concurrently on a pool of contexts; each catalogue must equal the reference's golden output
+for that snapshot, i.e. be the same in the mix as alone. A tight budget forces requests to
+wait for memory and idle workers to give their buffers back; the results do not change.
+"""
+from __future__ import annotations
+
+import threading
+
+import pytest
+
+from conftest import GOLDEN, golden
+
+pytestmark = pytest.mark.gpu
+
+MIX = ["w1_20k", "w1_20k_sinks", "w1_20k_border", "w1_24k_split2", "w2_250k", "w1_20k_spline80"]
+
+
+def _check(pg, name, cat, tmp_path):
+    g = golden(name)
+    assert cat.summary().strip() == g["summary"], name
+    d = tmp_path / name
+    d.mkdir()
+    cat.write_peaks(str(d / "res.txt"))
+    assert (d / g["peaks_file"]).read_bytes() == (GOLDEN / name / g["peaks_file"]).read_bytes(), name
+
+
+@pytest.mark.parametrize("workers,budget_of_largest", [(3, 0.0), (2, 1.2)])
+def test_mixed_requests_match_alone(workers, budget_of_largest, built, case_dir, tmp_path):
+    pg = built
+    cases_m = {n: case_dir(n) for n in MIX}
+    snaps = {n: pg.Snapshot(m["lis"]) for n, m in cases_m.items()}
+    params = {n: pg.params(m["param"]) for n, m in cases_m.items()}
+    budget = 0
+    if budget_of_largest:
+        largest = max(pg.lib().plan_footprint_bytes(s.n, None) for s in snaps.values())
+        budget = int(largest * budget_of_largest)
+    srv = pg.Server(0, workers, budget)
+    try:
+        ids = {}
+        lock = threading.Lock()
+
+        def submit(names):
+            for n in names:
+                rid = srv.submit(snaps[n], params[n])
+                with lock:
+                    ids[n] = rid
+
+        ts = [threading.Thread(target=submit, args=(MIX[k::2],)) for k in range(2)]
+        for t in ts:
+            t.start()
+        for t in ts:
+            t.join()
+        assert len(ids) == len(MIX)
+        for n in MIX:
+            got = srv.poll(ids[n], wait=True)
+            assert got is not None
+            cat, lat = got
+            assert lat > 0
+            _check(pg, n, cat, tmp_path / f"w{workers}")
+            cat.close()
+        st = srv.stats()
+        if budget:
+            assert st["peak_held_bytes"] <= budget
+    finally:
+        srv.close()
+        for s in snaps.values():
+            s.close()
+
+
+def test_oversized_request_is_refused(built, case_dir):
+    pg = built
+    m = case_dir("w1_20k")
+    snap = pg.Snapshot(m["lis"])
+    srv = pg.Server(0, 1, 1 << 20)  # 1 MiB: nothing fits
+    try:
+        with pytest.raises(pg.PlanError) as e:
+            srv.submit(snap, pg.params(m["param"]))
+        assert e.value.status == 6
+    finally:
+        srv.close()
+        snap.close()
