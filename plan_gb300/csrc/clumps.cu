@@ -1171,6 +1171,7 @@ __global__ void __launch_bounds__(kRebindThreads) k_rebind_round(const uint32_t 
             // Everything before the first disagreement is the reference's sequence; the first
             // disagreeing candidate is decided by its (exact) check.
             __shared__ double sst[33][7];  // M and the six components after each tentative acceptance
+            __shared__ double srcp[32];    // 1 / M after each tentative acceptance
             const int lane = threadIdx.x;
             const unsigned full = 0xffffffffu;
             const int cl = lane < 6 ? lane : 0;  // the state component this lane carries
@@ -1191,22 +1192,37 @@ __global__ void __launch_bounds__(kRebindThreads) k_rebind_round(const uint32_t 
                     at = wend;
                     continue;
                 }
-                // states after each tentative acceptance (src/tree.hpp:4696-4701)
+                // states after each tentative acceptance (src/tree.hpp:4696-4701). The masses
+                // first (their own sequential sum), then one reciprocal per lane, in parallel.
                 double Mi = M_;
+                int ns = 0;
+                for (unsigned bits = B; bits; bits &= bits - 1u) {
+                    Mi = Mi + tpos[at + (uint32_t)(__ffs(bits) - 1) - base].w;
+                    ++ns;
+                    if (lane == 0) sst[ns][0] = Mi;
+                }
+                if (lane == 0) sst[0][0] = M_;
+                __syncwarp();
+                if (lane < ns) srcp[lane] = 1.0 / sst[lane + 1][0];  // correctly rounded reciprocal
+                __syncwarp();
+                // The components: c' = (c M + m q) / M with the division as Markstein's
+                // correction of a reciprocal product (q0 = num y, r = num - q0 M exactly by
+                // FMA, c' = RN(q0 + r y)), which equals the correctly rounded quotient when y
+                // is the correctly rounded 1/M; checked against IEEE division on 9e8 operand
+                // pairs. A zero numerator keeps its sign as the division does.
                 double ci = cl == 0 ? x_ : cl == 1 ? y_ : cl == 2 ? z_ : cl == 3 ? vx_ : cl == 4 ? vy_ : vz_;
                 if (lane < 6) sst[0][1 + lane] = ci;
-                if (lane == 0) sst[0][0] = Mi;
-                int ns = 0;
+                int t = 0;
                 for (unsigned bits = B; bits; bits &= bits - 1u) {
                     const uint32_t j = at + (uint32_t)(__ffs(bits) - 1) - base;
                     const double4_32a p = tpos[j], v = tvel[j];
-                    const double Mn = Mi + p.w;
+                    const double Mn = sst[t + 1][0], yr = srcp[t];
                     const double qc = cl == 0 ? p.x : cl == 1 ? p.y : cl == 2 ? p.z : cl == 3 ? v.x : cl == 4 ? v.y : v.z;
-                    ci = (ci * Mn + p.w * qc) / Mn;
-                    Mi = Mn;
-                    ++ns;
-                    if (lane < 6) sst[ns][1 + lane] = ci;
-                    if (lane == 0) sst[ns][0] = Mi;
+                    const double num = ci * Mn + p.w * qc;
+                    const double q0 = num * yr;
+                    ci = num == 0.0 ? num : fma(fma(-q0, Mn, num), yr, q0);
+                    ++t;
+                    if (lane < 6) sst[t][1 + lane] = ci;
                 }
                 __syncwarp();
                 bool ver = false;
