@@ -349,6 +349,95 @@ def run_gpu(args) -> None:
         dist.destroy_process_group()
 
 
+# ---------------------------------------------------------------- serving (opt-in: --serve K)
+def serve_requests(k: int, max_log2: int, seed: int):
+    """K snapshots of the workload's mixture, sizes log-uniform in [2^16, 2^max_log2], clump
+    count proportional to N (the generator scales it), each with its own seed."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(2.0 ** 16), np.log(2.0 ** max_log2), k)).astype(np.int64)
+    return [(int(n), 1000 + i) for i, n in enumerate(sizes)]
+
+
+def latency_stats(lat_ms) -> dict:
+    return {"p50": float(np.percentile(lat_ms, 50)), "p99": float(np.percentile(lat_ms, 99)), "n": len(lat_ms)}
+
+
+class _ViewOnly:
+    """A snapshot given by its .lis view alone (records owned by the caller)."""
+
+    def __init__(self, view):
+        self.view = view
+
+
+def run_serve(args) -> None:
+    """Poisson arrivals of mixed-size snapshots through the serving loop (plan_submit /
+    plan_poll), and the same requests one by one through the plain path on one context.
+    Every served catalogue must equal the plain one; prints one JSON line."""
+    import torch
+
+    import plan_gb300 as pg
+
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py: no CUDA device (this path has no CPU fallback)")
+    reqs = []
+    with tempfile.TemporaryDirectory() as d:
+        for n, sd in serve_requests(args.serve, args.serve_max_log2, SEED):
+            rec, fourpig = make_records(n, sd, pinned=True)
+            par = Path(d) / f"para{sd}.txt"
+            write_params(par, fourpig, os.cpu_count() or 1)
+            reqs.append({"n": n, "rec": rec, "view": lis_view(pg, rec.data_ptr(), n), "param": pg.params(str(par))})
+    rng = np.random.default_rng(SEED + 7)
+    gaps = rng.exponential(1.0 / args.serve_rate, len(reqs))
+    # the plain path, one snapshot after another on one context (also the warm-up)
+    f = pg.Finder(0)
+    plain_lat, plain_sum = [], []
+    t0 = time.perf_counter()
+    for r in reqs:
+        t = time.perf_counter()
+        p = pg.Params.from_buffer_copy(r["param"])
+        cat = f.find_clumps(_ViewOnly(r["view"]), p)
+        plain_lat.append(1e3 * (time.perf_counter() - t))
+        plain_sum.append(cat.summary())
+        cat.close()
+    plain_s = time.perf_counter() - t0
+    f.close()
+    # served: arrivals on their Poisson schedule from a submitting thread
+    srv = pg.Server(0, args.serve_workers, 0)
+    ids = [None] * len(reqs)
+
+    def submitter():
+        for i, r in enumerate(reqs):
+            time.sleep(gaps[i])
+            ids[i] = srv.submit(_ViewOnly(r["view"]), pg.Params.from_buffer_copy(r["param"]))
+
+    clocks = ClockSampler(0)
+    clocks.start()
+    t0 = time.perf_counter()
+    th = threading.Thread(target=submitter)
+    th.start()
+    th.join()
+    served_lat, same = [], True
+    for i in range(len(reqs)):
+        cat, lat = srv.poll(ids[i], wait=True)
+        served_lat.append(lat)
+        same = same and cat.summary() == plain_sum[i]
+        cat.close()
+    served_s = time.perf_counter() - t0
+    clk = clocks.stop()
+    st = srv.stats()
+    srv.close()
+    n_tot = sum(r["n"] for r in reqs)
+    line = {"metric": "snapshots/s served", "value": len(reqs) / served_s, "unit": "snapshots/s", "n_gpus": 1,
+            "higher_is_better": True, "data": "synthetic", "dtype": "f64",
+            "config": {"workload": f"{len(reqs)} requests of the workload's mixture, N log-uniform in [2^16, 2^{args.serve_max_log2}], "
+                                   f"Poisson arrivals at {args.serve_rate}/s", "workers": args.serve_workers, "particles": n_tot},
+            "served": {"snapshots_per_s": len(reqs) / served_s, "particles_per_s": n_tot / served_s,
+                       "latency_ms": latency_stats(served_lat), "peak_held_bytes": st["peak_held_bytes"], "releases": st["releases"]},
+            "plain": {"snapshots_per_s": len(reqs) / plain_s, "particles_per_s": n_tot / plain_s, "latency_ms": latency_stats(plain_lat)},
+            "identical_catalogues": same, "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -358,8 +447,14 @@ def main() -> None:
     ap.add_argument("--n", type=int, default=N_FULL, help="particles per snapshot (default: the full workload)")
     ap.add_argument("--sample-n", type=int, default=1 << 22, help="particles of the CPU sample snapshot")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serve", type=int, default=0, help="instead: K requests through the serving loop (plan_submit/plan_poll)")
+    ap.add_argument("--serve-workers", type=int, default=3)
+    ap.add_argument("--serve-rate", type=float, default=4.0, help="Poisson arrivals per second")
+    ap.add_argument("--serve-max-log2", type=int, default=22, help="largest request 2^k particles")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.serve and args.impl == "gpu":
+        run_serve(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

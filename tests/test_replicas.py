@@ -55,3 +55,17 @@ def test_single_process_has_no_collective():
 
     assert bench.reduce_max(7.5, None) == 7.5
     assert bench.aggregate(1, 10, 2, 1000.0) == 20.0
+
+
+def test_serving_requests_and_latency_stats():
+    """The serving leg's request stream: sizes log-uniform in [2^16, 2^k], one seed each,
+    the same stream every run; p50/p99 from the latencies."""
+    import bench
+
+    a = bench.serve_requests(64, 20, 1)
+    assert a == bench.serve_requests(64, 20, 1)
+    sizes = [n for n, _ in a]
+    assert min(sizes) >= 1 << 16 and max(sizes) <= 1 << 20
+    assert len({sd for _, sd in a}) == 64
+    st = bench.latency_stats([1.0, 2.0, 3.0, 4.0])
+    assert st["p50"] == 2.5 and st["n"] == 4 and 3.9 < st["p99"] <= 4.0
