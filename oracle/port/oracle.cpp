@@ -407,7 +407,7 @@ void Tree::build(Params &p, std::vector<Particle> &parts, bool check_pos) {  // 
                 uint32_t e = b;
                 while (e < s.e && key_digit(sk[e], s.level) == o) ++e;
                 level_count[s.level]++;
-                if (!(e - b <= 8 || s.level == 31)) kids.push_back({s.level + 1, b, e});
+                if (!(e - b <= max_leaf_size || s.level == 31)) kids.push_back({s.level + 1, b, e});
                 b = e;
             }
             for (auto it = kids.rbegin(); it != kids.rend(); ++it) st.push_back(*it);
@@ -451,7 +451,7 @@ void Tree::build(Params &p, std::vector<Particle> &parts, bool check_pos) {  // 
             nd.half_width = f.hw;
             for (int k = 0; k < 3; ++k) nd.center[k] = f.c[k] + f.hw * kOrth[o][k];
             nd.orthant = (uint16_t)o;
-            if (!(e - b <= 8 || f.level == 31)) kids.push_back({f.level + 1, b, e, (uint32_t)d, nd.center, 0.5 * f.hw});
+            if (!(e - b <= max_leaf_size || f.level == 31)) kids.push_back({f.level + 1, b, e, (uint32_t)d, nd.center, 0.5 * f.hw});
             b = e;
         }
         // FillTree recurses into each branch before creating the next sibling, so node
@@ -597,6 +597,131 @@ void Tree::ball(const V3 &c, double r, std::vector<uint32_t> &out) const {  // s
             }
         }
     }
+}
+
+uint32_t Tree::ball_count_sheared(const V3 &c, double r, const V3 &max_distance, double shear_distance, const Params &p) const {
+    const double diag_f = std::sqrt(3);  // to_diagonal
+    uint32_t count = 0;
+    std::vector<uint32_t> st{0};
+    while (!st.empty()) {
+        const uint32_t node = st.back();
+        st.pop_back();
+        const Node &nd = nodes[node];
+        // ShearedCenter2Center (src/tree.hpp:3308-3331): the node's image across the x
+        // faces also moves in y by the shear, which the y component then sees
+        V3 nc = nd.center, c2c;
+        for (int i = 0; i < 3; ++i) {
+            c2c[i] = c[i] - nc[i];
+            if (std::fabs(c2c[i]) > max_distance[i]) {
+                if (c2c[i] > 0) c2c[i] -= p.box_length[i];
+                else c2c[i] += p.box_length[i];
+                if (i == 0) {
+                    if (c[0] < 0) {
+                        nc[1] -= shear_distance;
+                        nc[1] += static_cast<int>((p.box_max[1] - nc[1]) / p.box_length[1]) * p.box_length[1];
+                    } else {
+                        nc[1] += shear_distance;
+                        nc[1] -= static_cast<int>((nc[1] - p.box_min[1]) / p.box_length[1]) * p.box_length[1];
+                    }
+                }
+            }
+        }
+        // SphereContainNodeWithShear (src/tree.hpp:3335-3346)
+        const double tmp = nd.half_width * diag_f;
+        V3 td;
+        for (int i = 0; i < 3; ++i) td[i] = std::fabs(c2c[i]) + tmp;
+        if (norm2(td) < r * r) {
+            count += nd.end - nd.begin;
+            continue;
+        }
+        // SphereNodeIntersectWithShear (src/tree.hpp:3350-3380)
+        const double cd = norm2(c2c), tr = tmp + r;
+        if (cd > tr * tr) continue;
+        bool hit = cd < r || cd < nd.half_width;
+        if (!hit) {
+            double m2 = 0;
+            for (int d = 0; d < 3; ++d) {
+                const double lo = (c[d] - c2c[d]) - nd.half_width, hi = (c[d] - c2c[d]) + nd.half_width;
+                if (c[d] < lo) m2 += (c[d] - lo) * (c[d] - lo);
+                else if (c[d] > hi) m2 += (c[d] - hi) * (c[d] - hi);
+            }
+            hit = m2 <= r * r;
+        }
+        if (!hit) continue;
+        if (nd.num_daughters == 0) {  // the points themselves are compared without the image
+            for (uint32_t q = nd.begin; q != nd.end; ++q)
+                if (norm2(sub(c, pts[q].pos)) <= r * r) ++count;
+        } else {
+            for (int d = nd.num_daughters - 1; d >= 0; --d) st.push_back(nd.first_daughter + d);
+        }
+    }
+    return count;
+}
+
+DensityVsScale density_vs_scale(const Tree &t, const Params &p, double time) {
+    DensityVsScale out;
+    // z range: from the cell centre at the box centre down past the lowest point, up to the
+    // highest point (RecursiveFindExtreme finds the extreme values exactly)
+    double zlo = t.pts[0].pos[2], zhi = t.pts[0].pos[2];
+    for (const auto &q : t.pts) {
+        zlo = std::min(zlo, q.pos[2]);
+        zhi = std::max(zhi, q.pos[2]);
+    }
+    double z_min = p.box_center[2] - p.cell_length[2] / 2.0;
+    const double z_max = zhi;
+    while (z_min - p.cell_length[2] > zlo) z_min -= p.cell_length[2];
+    const int num_levels = (int)std::round(std::log10(p.box_half_width[0] * 2 / p.cell_length[0]) / std::log10(2.0)) + 1;
+    out.radii.assign(num_levels, p.cell_length[0] / 2.0);
+    out.max_rhop.assign(num_levels, 0.0);
+    std::vector<V3> maxd(num_levels);
+    const double shear = p.shear_speed * time;
+    for (int i = 0; i < num_levels; ++i) {
+        out.radii[i] *= std::pow(2.0, i);
+        for (int d = 0; d < 3; ++d) maxd[i][d] = p.box_length[d] - out.radii[i];
+        maxd[i][2] = 100 * p.max_half_width;  // no periodic search in z
+    }
+    const V3 cmin(p.box_min[0] + 0.5 * p.cell_length[0], p.box_min[1] + 0.5 * p.cell_length[1], p.box_min[2] + 0.5 * p.cell_length[2]);
+    const V3 step = p.cell_length, sub1 = div(step, 2.0), sub2 = div(step, 4.0);
+    for (double z = z_min; z < z_max; z += step[2]) {
+        for (double y = cmin[1]; y < p.box_max[1]; y += step[1]) {
+            for (double x = cmin[0]; x < p.box_max[0]; x += step[0]) {
+                const V3 c(x, y, z);
+                for (int i = 0; i < num_levels; ++i) {
+                    double &mx = out.max_rhop[i];
+                    uint32_t n = t.ball_count_sheared(c, out.radii[i], maxd[i], shear, p);
+                    if (n > mx) mx = n;
+                    if (i >= 3) continue;
+                    for (int o = 0; o < 8; ++o) {  // the eight sub-centres
+                        V3 sc;
+                        for (int d = 0; d < 3; ++d) sc[d] = c[d] + sub1[d] * kOrth[o][d];
+                        n = t.ball_count_sheared(sc, out.radii[i], maxd[i], shear, p);
+                        if (n > mx) mx = n;
+                        if (i == 0) {
+                            // the reference's inner loop offsets by the outer orthant eight
+                            // times (src/analyses.hpp:296-305): one more centre per orthant
+                            V3 ss;
+                            for (int d = 0; d < 3; ++d) ss[d] = sc[d] + sub2[d] * kOrth[o][d];
+                            n = t.ball_count_sheared(ss, out.radii[i], maxd[i], shear, p);
+                            if (n > mx) mx = n;
+                        }
+                    }
+                }
+            }
+        }
+    }
+    std::ostringstream h, l;
+    h << std::setw(15) << std::setfill(' ') << "#time";
+    for (double r : out.radii) h << std::setw(15) << std::setfill(' ') << std::scientific << r;
+    h << "\n";
+    l << std::setw(15) << std::setfill(' ') << std::scientific << time;
+    for (int i = 0; i < num_levels; ++i) {
+        out.max_rhop[i] *= (p.mass_per_particle[0] / (4.1887902047863910 * std::pow(out.radii[i], 3)));
+        l << std::setw(15) << std::setfill(' ') << std::scientific << out.max_rhop[i];
+    }
+    l << "\n";
+    out.header = h.str();
+    out.line = l.str();
+    return out;
 }
 
 uint32_t Tree::ball_count(const V3 &c, double r) const {

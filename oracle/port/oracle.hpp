@@ -141,6 +141,7 @@ struct Tree {
     V3 boxmin, scale;
     V3 cell_length, half_cell_length, cell_length_squared, three_half_cell_length;
     uint64_t check_outside = 0;  // points found outside their node by the tree check
+    uint32_t max_leaf_size = 8;  // BHtree::max_leaf_size (64 under --Density_Vs_Scale)
 
     // BuildTree (src/tree.hpp:2759-2908). `parts` is consumed.
     void build(Params &p, std::vector<Particle> &parts, bool check_pos);
@@ -158,7 +159,19 @@ struct Tree {
     void ball(const V3 &c, double r, std::vector<uint32_t> &out) const;
     uint32_t ball_count(const V3 &c, double r) const;
     double quadratic_spline(V3 d) const;
+    // RecursiveBallSearchCountWithShear (src/tree.hpp:3306-3402): points within r of c, the
+    // nodes compared through their shearing-periodic image where far away
+    uint32_t ball_count_sheared(const V3 &c, double r, const V3 &max_distance, double shear_distance, const Params &p) const;
 };
+
+// BasicAnalysesWithTree for --Density_Vs_Scale (src/analyses.hpp:196-333): the largest
+// count of points within each search radius over the cell centres (and sub-centres for the
+// three smallest radii), as a density. `header` is the first snapshot's header line.
+struct DensityVsScale {
+    std::vector<double> radii, max_rhop;
+    std::string header, line;
+};
+DensityVsScale density_vs_scale(const Tree &t, const Params &p, double time);
 
 // ---------------------------------------------------------------- clumps
 struct Clump {  // Planetesimal, src/tree.hpp:4351-4809

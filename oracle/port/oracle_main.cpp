@@ -99,9 +99,14 @@ int main(int argc, char **argv) {
 #endif
     if (nthreads <= 0) nthreads = 1;
     bool first = true;
-    std::string stem = out.substr(0, out.find_last_of('.')) + "_planetesimals.txt";
-    FILE *pf = std::fopen(stem.c_str(), "w");
-    if (!pf) return 3;
+    if (!f_find && !f_basic && !f_dvs && !f_tmp) f_find = 1;  // src/global.cpp:498-501
+    const std::string ostem = out.substr(0, out.find_last_of('.'));
+    // result files in BasicAnalysesPreWork's order (src/analyses.cpp:16-33); with only
+    // --Density_Vs_Scale the basic results go to the first open file, the RMPL one
+    FILE *rf = nullptr, *pf = nullptr;
+    if (f_dvs && !(rf = std::fopen((ostem + "_RMPL.txt").c_str(), "w"))) return 3;
+    if (f_find && !(pf = std::fopen((ostem + "_planetesimals.txt").c_str(), "w"))) return 3;
+    FILE *basic_file = pf ? pf : rf;
     for (int num = start; num <= end; num += step) {
         std::ostringstream nn;
         nn << std::setw(4) << std::setfill('0') << num;
@@ -118,6 +123,10 @@ int main(int argc, char **argv) {
         int rc = read_lis_files(files, snap);
         if (rc) return rc;
         finish_read(snap, par, first);
+        if (f_dvs) {  // BasicAnalyses' settings for --Density_Vs_Scale (src/analyses.hpp:29-33)
+            par.max_ghost_zone_width = par.max_half_width;
+            f_noghost = 1;
+        }
         uint32_t nin = snap.num_particles;
         double t1 = now();
         if (!f_noghost) make_ghosts(snap, par);
@@ -126,8 +135,16 @@ int main(int argc, char **argv) {
         f.threads = nthreads;
         f.pow_mode = pow_mode ? POW_CORRECT : POW_LIBM;
         f.time = snap.time;
-        f.stream_scientific = !first;
+        // the shared summary stream is left scientific by an earlier snapshot's basic results
+        // or by this snapshot's density-vs-scale lines
+        f.stream_scientific = !first || f_dvs;
+        if (f_dvs) f.tree.max_leaf_size = 64;
         f.tree.build(par, snap.parts, true);
+        if (f_dvs) {
+            DensityVsScale dv = density_vs_scale(f.tree, par, snap.time);
+            const std::string txt = (first ? dv.header : std::string()) + dv.line;
+            std::fwrite(txt.data(), 1, txt.size(), rf);
+        }
         double t2 = now();
         std::string summary = f.find(nin);
         double t3 = now();
@@ -139,10 +156,11 @@ int main(int argc, char **argv) {
             write_parlists("ParList." + sid.str(), f, sampling);
         }
         std::string line = (first ? basic_results_header() : std::string()) + basic_results_line(f, par, snap.time);
-        std::fwrite(line.data(), 1, line.size(), pf);
+        std::fwrite(line.data(), 1, line.size(), basic_file);
         std::fprintf(stderr, "[oracle] read %.4f s, ghost+tree %.4f s, find %.4f s, tree points %u, threads %d\n", t1 - t0, t2 - t1, t3 - t2, f.tree.size(), nthreads);
         first = false;
     }
-    std::fclose(pf);
+    if (pf) std::fclose(pf);
+    if (rf) std::fclose(rf);
     return 0;
 }

@@ -2,10 +2,12 @@
 //
 // This file is oracle code: it links src/global.cpp, src/tree.cpp and src/tree.hpp of the
 // reference exactly as they are and drives the same per-snapshot sequence as the
-// reference's main program for `--Find_Clumps` (src/main.cpp:39-102), minus the grid
-// analyses of src/analyses.hpp, which need a working Boost.MultiArray and never touch the
-// clump catalogue. Only tests/, bench.py's CPU-baseline leg and __graft_entry__.smoke() may
-// run what this builds.
+// reference's main program for `--Find_Clumps` and `--Density_Vs_Scale`
+// (src/main.cpp:39-102). Of src/analyses.hpp it runs BasicAnalysesWithTree as it is; the
+// part of BasicAnalyses that --Density_Vs_Scale needs (three settings, src/analyses.hpp:29-33)
+// is repeated here because the rest of that function needs a working Boost.MultiArray (the
+// grid analyses, which never touch these outputs). Only tests/, bench.py's CPU-baseline leg
+// and __graft_entry__.smoke() may run what this builds.
 //
 // Extra, optional behaviour (never changes the catalogue): when PLAN_REF_DUMP=<dir> is set,
 // stage arrays are written as raw little-endian binaries after each public call, using only
@@ -22,7 +24,9 @@
 //                 J[3] f64, then n member tree indices (u32) in `indices` order
 #include "global.hpp"
 #include "tree.hpp"
+#include "analyses.hpp"
 
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
@@ -129,13 +133,22 @@ int main(int argc, const char *argv[]) {
     mpi->DetermineLoop(progIO->num_files);
     const char *dump = std::getenv("PLAN_REF_DUMP");
     DataSet<float, dim> ds;
+    const bool dvs = progIO->flags.density_vs_scale_flag != 0;
+    // result files in BasicAnalysesPreWork's order (src/analyses.cpp:16-33)
+    if (dvs) mpi->OpenFile(progIO->file_name.max_rhop_vs_scale_file);
     if (progIO->flags.find_clumps_flag) mpi->OpenFile(progIO->file_name.planetesimals_file);
     for (int lc = mpi->loop_begin; lc <= mpi->loop_end; lc += mpi->loop_step) {
         double t0 = Timer::GetCurrentTime();
         ds.particle_set.ReadLisFile(lc);
+        if (dvs) {  // BasicAnalyses' settings for --Density_Vs_Scale (src/analyses.hpp:29-33)
+            progIO->numerical_parameters.max_ghost_zone_width = progIO->numerical_parameters.max_half_width;
+            ds.tree.max_leaf_size = std::pow(1U << dim, 2);
+            progIO->flags.no_ghost_particle_flag = 1;
+        }
         double t1 = Timer::GetCurrentTime();
         ds.particle_set.MakeGhostParticles(progIO->numerical_parameters);
         ds.tree.BuildTree(progIO->numerical_parameters, ds.particle_set);
+        if (dvs) BasicAnalysesWithTree(ds, lc);
         double t2 = Timer::GetCurrentTime();
         ds.tree.FindPlanetesimals(ds, lc);
         ds.planetesimal_list.WriteBasicResults(lc);

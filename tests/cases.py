@@ -75,6 +75,14 @@ VARIANTS = [
      ["-y", "0.09,-0.06", "-z", "-0.06,0.05", "--No_Ghost", "--Save_Clumps"]),
     ("w1_20k_box_all", Case("w1_20k", 1, 20000, 5, 32), ["-x", "-0.2,0.2"]),
 ]
+# --Density_Vs_Scale runs (src/analyses.hpp:196-333): the sheared ball counts at every cell
+# centre, written to <out>_RMPL.txt, and the clump finder on that run's tree (64-point leaves,
+# no ghosts, doubled root box); alone, the flag sends the basic results into the RMPL file
+DVS = [
+    ("w1_20k_dvs16", Case("w1_20k_dvs16", 1, 20000, 41, 16), ["--Density_Vs_Scale", "--Save_Clumps"]),
+    ("w1_20k_dvs16_find", Case("w1_20k_dvs16", 1, 20000, 41, 16), ["--Density_Vs_Scale", "--Find_Clumps"]),
+    ("w1_20k_dvs32_sheared", Case("w1_20k_dvs32s", 1, 20000, 43, 32, edit="border", time=0.37), ["--Density_Vs_Scale"]),
+]
 # one run over two snapshot files (-f 0:1): the second is later in time and uses the first's box
 MULTI = [Case("multi_0", 1, 20000, 5, 32), Case("multi_1", 1, 20000, 6, 32, time=0.25)]
 

@@ -168,6 +168,30 @@ def variants() -> None:
             print(f"{name}: {meta['summary']} ({len(meta['parlist'])} member lists)")
 
 
+def dvs_variants() -> None:
+    """--Density_Vs_Scale runs of the reference's CLI: every file it writes, byte for byte."""
+    for name, c, extra in cases.DVS:
+        with tempfile.TemporaryDirectory() as tmp:
+            tmp = Path(tmp)
+            m = cases.materialise(c, tmp / "in")
+            out = tmp / "ref"
+            out.mkdir()
+            r = subprocess.run([str(REF)] + cases.cli_args(m, str(out / "res.txt")) + extra, cwd=out, capture_output=True, text=True,
+                               check=True)
+            g = HERE / name
+            if g.exists():
+                shutil.rmtree(g)
+            g.mkdir()
+            files = sorted(p.name for p in out.iterdir() if p.is_file())
+            for f in files:
+                shutil.copy(out / f, g / f)
+            summary = [ln for ln in r.stdout.splitlines() if "Finish clump finding" in ln]
+            meta = {"case": name, "lis_sha256": m["sha256"], "args": extra, "summary": summary, "files": files,
+                    "parlist": cases.parlist_digests(out)}
+            (g / "meta.json").write_text(json.dumps(meta, indent=1) + "\n")
+            print(f"{name}: {files} {summary}")
+
+
 def main() -> None:
     if not REF.exists():
         sys.exit(f"{REF} missing: run `make -C oracle ref` in a checkout with the reference")
@@ -176,6 +200,8 @@ def main() -> None:
         multi_snapshot()
     if not only or "variants" in only:
         variants()
+    if not only or "dvs" in only:
+        dvs_variants()
     for c in cases.CASES + cases.SPLINE:
         if only and c.name not in only:
             continue

@@ -157,3 +157,27 @@ def test_oracle_cli_variants(name, case, extra, oracle_mod, tmp_path):
     assert (out / meta["peaks_file"]).read_bytes() == (g / meta["peaks_file"]).read_bytes()
     assert (out / "res_planetesimals.txt").read_bytes() == (g / "planetesimals.txt").read_bytes()
     assert cases.parlist_digests(out) == meta["parlist"]
+
+
+@pytest.mark.parametrize("name,case,extra", cases.DVS, ids=[v[0] for v in cases.DVS])
+def test_oracle_cli_density_vs_scale(name, case, extra, oracle_mod, tmp_path):
+    """--Density_Vs_Scale (src/analyses.hpp:196-333, src/main.cpp:71-79): the RMPL file of
+    sheared ball counts, then the clump finder on that run's tree (64-point leaves, no
+    ghosts, doubled root box), with the basic results in the RMPL file when the flag is
+    alone. Every file the reference wrote must come out byte for byte."""
+    import json
+    import subprocess
+
+    g = GOLDEN / name
+    meta = json.loads((g / "meta.json").read_text())
+    m = cases.materialise(case, tmp_path / "in")
+    assert m["sha256"] == meta["lis_sha256"]
+    out = tmp_path / "out"
+    out.mkdir()
+    r = subprocess.run([str(oracle_mod.CLI)] + cases.cli_args(m, str(out / "res.txt")) + extra, cwd=out, capture_output=True, text=True,
+                       check=True)
+    assert [ln for ln in r.stdout.splitlines() if "Finish clump finding" in ln] == meta["summary"]
+    assert sorted(p.name for p in out.iterdir() if p.is_file()) == meta["files"]
+    for f in meta["files"]:
+        assert (out / f).read_bytes() == (g / f).read_bytes(), f
+    assert cases.parlist_digests(out) == meta["parlist"]
