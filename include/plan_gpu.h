@@ -67,6 +67,8 @@ typedef struct plan_params {
     int32_t no_ghost;               /* --No_Ghost */
     int32_t user_box;               /* -x/-y/-z given (src/global.cpp:398-440) */
     double user_box_min[3], user_box_max[3]; /* their limits, lo <= hi; 0,0 on an axis = the box's extent */
+    int32_t density_vs_scale;       /* --Density_Vs_Scale: the tree is built as that analysis
+                                       wants it (64-point leaves, no ghosts, ghost zone = box) */
 } plan_params;
 
 /* Defaults of NumericalParameters (src/global.hpp:686-862). */
@@ -151,6 +153,14 @@ int plan_catalogue_write_parlists(plan_ctx *ctx, const plan_catalogue *cat, int 
 /* PlanetesimalList::WriteBasicResults (src/tree.hpp:4935-4953): the line for this snapshot
  * (with the header first when with_header != 0) into buf; returns the length or -1. */
 int plan_catalogue_basic_results(const plan_catalogue *cat, const plan_params *p, int with_header, char *buf, size_t cap);
+
+/* BasicAnalysesWithTree for --Density_Vs_Scale (src/analyses.hpp:196-333) on the tree of the
+ * last plan_build_tree, which must have had p->density_vs_scale set (64-point leaves, no
+ * ghosts): the search radii (half a cell times 1, 2, 4, ...) and, for each, the largest
+ * count of points within that radius of a cell centre or sub-centre as a density
+ * (count m / (4 pi / 3 r^3)). time = the snapshot's time (shear of the periodic images).
+ * Writes up to cap values to radii and rho; *nlev = the number of radii. */
+int plan_density_vs_scale(plan_ctx *ctx, const plan_params *p, double time, double *radii, double *rho, int cap, int *nlev);
 
 /* ---------------------------------------------------------------- serving
  * New, no counterpart in the reference (which processes its snapshot list one by one):

@@ -53,7 +53,7 @@ class Params(C.Structure):
         ("grav_constant", C.c_double), ("shear_speed", C.c_double), ("min_trusted_mass", C.c_double),
         ("ntypes", C.c_uint32), ("mass_per_particle", C.c_double * 16), ("mass_fraction_per_species", C.c_double * 16),
         ("box_set", C.c_int32), ("no_ghost", C.c_int32), ("user_box", C.c_int32), ("user_box_min", C.c_double * 3),
-        ("user_box_max", C.c_double * 3),
+        ("user_box_max", C.c_double * 3), ("density_vs_scale", C.c_int32),
     ]
 
 

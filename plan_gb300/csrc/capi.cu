@@ -366,6 +366,37 @@ int plan_morton_order_noalloc(plan_ctx *h, const uint32_t *keys3, uint32_t n, ui
     return c.status_from(rc, "plan_morton_order_noalloc");
 }
 
+int plan_density_vs_scale(plan_ctx *h, const plan_params *p, double time, double *radii, double *rho, int cap, int *nlev) {
+    if (!h || !p || !nlev) return kErrArgument;
+    Context &c = h->c;
+    g_ctx = &c;
+    c.last_error.clear();
+    cudaSetDevice(c.device);
+    if (!c.tree.Tu) {
+        c.last_error = "plan_density_vs_scale: no tree (call plan_build_tree first)";
+        return kErrArgument;
+    }
+    std::vector<double> r, v;
+    cudaMemsetAsync(c.d_err, 0, 16, c.stream);
+    int rc = density_vs_scale(c, *p, time, r, v, c.stream);
+    if (rc == kOk) {
+        unsigned err = 0;
+        cudaMemcpy(&err, c.d_err, 4, cudaMemcpyDeviceToHost);
+        if (err) {
+            c.last_error = "device error flags " + std::to_string(err) + " in the ball counts";
+            rc = kErrDeviceLimit;
+        }
+    }
+    if (rc == kOk) {
+        *nlev = (int)r.size();
+        for (int i = 0; i < (int)r.size() && i < cap; ++i) {
+            if (radii) radii[i] = r[i];
+            if (rho) rho[i] = v[i];
+        }
+    }
+    return c.status_from(rc, "plan_density_vs_scale");
+}
+
 int plan_catalogue_write_parlists(plan_ctx *h, const plan_catalogue *cat, int file_number, uint32_t sampling) {
     if (!h || !cat) return kErrArgument;
     Context &c = h->c;

@@ -288,23 +288,28 @@ __global__ void k_sortpoints(const uint32_t *starts, uint32_t Tu, uint32_t T, co
 }
 
 // ---------------------------------------------------------------- octree
+// LEAF = max_leaf_size: 8 by default, 64 for the particle tree of --Density_Vs_Scale runs
+template <uint32_t LEAF>
 __global__ void k_lcp(const uint32_t *k0, const uint32_t *k1, const uint32_t *k2, uint32_t n, uint8_t *lcp_prev, uint8_t *win) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int a = 0;
     if (i > 0) a = key_lcp_digits(k0[i - 1], k1[i - 1], k2[i - 1], k0[i], k1[i], k2[i]);
     lcp_prev[i] = (uint8_t)min(a, 31);
-    // 9-key window starting at i: lcp of its first and last key
-    win[i] = (i + 8 < n) ? (uint8_t)min(key_lcp_digits(k0[i], k1[i], k2[i], k0[i + 8], k1[i + 8], k2[i + 8]), 31) : (uint8_t)255;
+    // (LEAF + 1)-key window starting at i: lcp of its first and last key
+    win[i] = (i + LEAF < n) ? (uint8_t)min(key_lcp_digits(k0[i], k1[i], k2[i], k0[i + LEAF], k1[i + LEAF], k2[i + LEAF]), 31)
+                            : (uint8_t)255;
 }
 
-// leaf digit level: the node at digit level L containing i is internal iff some window of 9
-// consecutive keys containing i shares L digits (CountNodesLeaves' count > 8 rule).
+// leaf digit level: the node at digit level L containing i is internal iff some window of
+// LEAF + 1 consecutive keys containing i shares L digits (CountNodesLeaves' count > max_leaf_size
+// rule, src/tree.hpp:2674).
+template <uint32_t LEAF>
 __global__ void k_leaf_level(const uint8_t *win, uint32_t n, uint8_t *leaf_lvl) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int M = 0;
-    uint32_t j0 = i >= 8 ? i - 8 : 0;
+    uint32_t j0 = i >= LEAF ? i - LEAF : 0;
     for (uint32_t j = j0; j <= i; ++j) {
         uint8_t w = win[j];
         if (w != 255 && w > M) M = w;
@@ -461,7 +466,8 @@ __global__ void k_node_end_level(uint32_t first, uint32_t count, const uint32_t 
 // the tree come from the snapshot arena; temporaries from the scratch arena, released on
 // return.
 int build_octree(Context &c, double4_32a *in_pos, double4_32a *in_vel, const uint32_t *in_type, uint32_t T, const TreeBox &box,
-                 const double *mass_table, uint32_t ntypes, DevTree &tr, cudaStream_t s, cudaEvent_t after_sort) {
+                 const double *mass_table, uint32_t ntypes, DevTree &tr, cudaStream_t s, cudaEvent_t after_sort, uint32_t leaf) {
+    if (leaf != 8 && leaf != 64) return kErrArgument;
     Arena &A = c.arena;
     Arena &S = c.scratch;
     const size_t mark = S.used;
@@ -546,8 +552,13 @@ int build_octree(Context &c, double4_32a *in_pos, double4_32a *in_vel, const uin
     uint32_t *bc = S.get<uint32_t>((size_t)nb * 32);
     uint32_t *d_lc = S.get<uint32_t>(32);
     if (!lcp_prev || !win || !leaf_lvl || !bc || !d_lc) return kErrOutOfMemory;
-    k_lcp<<<nb, 256, 0, s>>>(tr.tk0, tr.tk1, tr.tk2, Tu, lcp_prev, win);
-    k_leaf_level<<<nb, 256, 0, s>>>(win, Tu, leaf_lvl);
+    if (leaf == 64) {
+        k_lcp<64><<<nb, 256, 0, s>>>(tr.tk0, tr.tk1, tr.tk2, Tu, lcp_prev, win);
+        k_leaf_level<64><<<nb, 256, 0, s>>>(win, Tu, leaf_lvl);
+    } else {
+        k_lcp<8><<<nb, 256, 0, s>>>(tr.tk0, tr.tk1, tr.tk2, Tu, lcp_prev, win);
+        k_leaf_level<8><<<nb, 256, 0, s>>>(win, Tu, leaf_lvl);
+    }
     k_level_block_counts<<<nb, 256, 0, s>>>(lcp_prev, leaf_lvl, Tu, bc);
     PLAN_CUDA(cudaMemsetAsync(d_lc, 0, 32 * 4, s));
     k_level_scan<<<32, 1024, 0, s>>>(bc, nb, d_lc);
@@ -691,6 +702,12 @@ int build_tree(Context &c, const plan_lis_view &v, plan_params &p, int first_fil
             p.mass_per_particle[t] = p.mass_fraction_per_species[t] * p.mass_total_code_units / N;
         }
         p.box_set = 1;
+    }
+    // --Density_Vs_Scale runs build this tree with 64-point leaves, no ghosts and the ghost
+    // zone as wide as the box (BasicAnalyses, src/analyses.hpp:29-33, run after the read)
+    if (p.density_vs_scale) {
+        p.max_ghost_zone_width = p.max_half_width;
+        p.no_ghost = 1;
     }
     // user box (src/tree.hpp:1585-1620): an axis given as 0,0 takes the box's extent; a box
     // that holds the whole domain changes nothing; otherwise only the particles inside it
@@ -851,7 +868,7 @@ int build_tree(Context &c, const plan_lis_view &v, plan_params &p, int first_fil
         MassTable mt;
         mt.ntypes = std::max<uint32_t>(1, std::min<uint32_t>(p.ntypes, 16));
         for (int t = 0; t < 16; ++t) mt.m[t] = p.mass_per_particle[t];
-        int rc = build_octree(c, in_pos, in_vel, in_type, T, box, mt.m, mt.ntypes, c.tree, s, ev[3]);
+        int rc = build_octree(c, in_pos, in_vel, in_type, T, box, mt.m, mt.ntypes, c.tree, s, ev[3], p.density_vs_scale ? 64u : 8u);
         if (rc) return rc;
     }
     if (selected) {

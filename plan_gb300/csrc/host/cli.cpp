@@ -3,9 +3,10 @@
 // Same command line (src/global.cpp:247-289, usage 558-578), same file names
 // (src/global.cpp:620-675) and the same outputs: <out-stem>_planetesimals.txt
 // (WriteBasicResults), peaks_at_<time>.txt and, with --Save_Clumps, ParList.<NNNN>/.
-// -x/-y/-z user boxes restrict the particles read, as in the reference. Grid analyses
-// (--Basic_Analyses, --Density_Vs_Scale, --Temp_Calculation) are not part of this build and
-// are rejected with exit code 2.
+// -x/-y/-z user boxes restrict the particles read, as in the reference. --Density_Vs_Scale
+// writes <out>_RMPL.txt and finds clumps on that run's tree, as the reference does. The grid
+// analyses (--Basic_Analyses, --Temp_Calculation) are not part of this build and are rejected
+// with exit code 2.
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -162,14 +163,16 @@ int main(int argc, char **argv) {
         std::cerr << "\nSomething is wrong with the argument list. Check usage by --Help or -h.\n";
         return 2;
     }
-    if (f_basic || f_dvs || f_tmp) {
-        std::cerr << "Error: only --Find_Clumps is available in this build (grid analyses are not part of it)." << std::endl;
+    if (f_basic || f_tmp) {
+        std::cerr << "Error: only --Find_Clumps and --Density_Vs_Scale are available in this build (the grid analyses are not part of it)."
+                  << std::endl;
         return 2;
     }
     if (dir.empty() || *dir.rbegin() != '/') dir.push_back('/');
     plan_params par;
     plan_params_init(&par);
     par.no_ghost = f_noghost;
+    par.density_vs_scale = f_dvs ? 1 : 0;
     par.user_box = user_box ? 1 : 0;
     for (int d = 0; d < 3; ++d) {
         par.user_box_min[d] = box_lo[d];
@@ -185,13 +188,24 @@ int main(int argc, char **argv) {
         std::cerr << "Error: no usable CUDA device (this program has no CPU path)." << std::endl;
         return exit_code(rc);
     }
-    std::string stem = out.substr(0, out.find_last_of('.')) + "_planetesimals.txt";
-    FILE *pf = std::fopen(stem.c_str(), "w");
-    if (!pf) {
-        std::cerr << "Error: Failed to open file " << stem << std::endl;
-        plan_ctx_destroy(ctx);
-        return 3;
+    // result files in BasicAnalysesPreWork's order (src/analyses.cpp:16-33): <out>_RMPL.txt for
+    // --Density_Vs_Scale, <out>_planetesimals.txt for --Find_Clumps; WriteBasicResults writes to
+    // the first open file when only the former is open
+    const std::string ostem = out.substr(0, out.find_last_of('.'));
+    FILE *rf = nullptr, *pf = nullptr;
+    for (int k = 0; k < 2; ++k) {
+        if (k == 0 ? !f_dvs : !f_find) continue;
+        const std::string name = ostem + (k == 0 ? "_RMPL.txt" : "_planetesimals.txt");
+        FILE *fh = std::fopen(name.c_str(), "w");
+        if (!fh) {
+            std::cerr << "Error: Failed to open file " << name << std::endl;
+            if (rf) std::fclose(rf);
+            plan_ctx_destroy(ctx);
+            return 3;
+        }
+        (k == 0 ? rf : pf) = fh;
     }
+    FILE *basic_file = pf ? pf : rf;
     const char *pd_env = std::getenv("PLAN_PARLIST_DEVICE");
     const bool parlist_device = pd_env && *pd_env == '1';
     std::ostringstream oc;  // keeps its formatting state across snapshots, as the reference's
@@ -216,7 +230,30 @@ int main(int argc, char **argv) {
         plan_lis_view view;
         plan_lis_get_view(lis, &view);
         plan_catalogue *cat = nullptr;
-        rc = plan_find_clumps(ctx, &view, &par, first ? 1 : 0, nullptr, &cat);
+        if (f_dvs) {
+            // BuildTree, BasicAnalysesWithTree, FindPlanetesimals (src/main.cpp:71-79)
+            rc = plan_build_tree(ctx, &view, &par, first ? 1 : 0, nullptr);
+            double radii[32], rho[32];
+            int nlev = 0;
+            if (!rc) rc = plan_density_vs_scale(ctx, &par, view.time, radii, rho, 32, &nlev);
+            if (!rc) {
+                std::ostringstream rm;  // src/analyses.hpp:258-266, 323-329
+                if (first) {
+                    rm << std::setw(15) << std::setfill(' ') << "#time";
+                    for (int i = 0; i < nlev && i < 32; ++i) rm << std::setw(15) << std::setfill(' ') << std::scientific << radii[i];
+                    rm << "\n";
+                }
+                rm << std::setw(15) << std::setfill(' ') << std::scientific << view.time;
+                for (int i = 0; i < nlev && i < 32; ++i) rm << std::setw(15) << std::setfill(' ') << std::scientific << rho[i];
+                rm << "\n";
+                const std::string t = rm.str();
+                std::fwrite(t.data(), 1, t.size(), rf);
+                oc << std::scientific;  // the shared stream is left scientific before the summary
+                rc = plan_find_planetesimals(ctx, &par, nullptr, &cat);
+            }
+        } else {
+            rc = plan_find_clumps(ctx, &view, &par, first ? 1 : 0, nullptr, &cat);
+        }
         if (rc) {
             std::cerr << "Error: " << plan_last_error(ctx) << std::endl;
             plan_lis_free(lis);
@@ -246,12 +283,13 @@ int main(int argc, char **argv) {
         if (rc) status = rc;
         char buf[1024];
         int len = plan_catalogue_basic_results(cat, &par, first ? 1 : 0, buf, sizeof(buf));
-        if (len > 0) std::fwrite(buf, 1, (size_t)len, pf);
+        if (len > 0) std::fwrite(buf, 1, (size_t)len, basic_file);
         plan_catalogue_free(cat);
         plan_lis_free(lis);
         first = false;
     }
-    std::fclose(pf);
+    if (pf) std::fclose(pf);
+    if (rf) std::fclose(rf);
     plan_ctx_destroy(ctx);
     return exit_code(status);
 }

@@ -100,10 +100,13 @@ int build_tree(Context &c, const plan_lis_view &v, plan_params &p, int first_fil
 // Keys, sort, sinks and octree for points in input order (pos.w = mass unless a mass
 // table is given); used for the particle tree and the clump trees.
 int build_octree(Context &c, double4_32a *in_pos, double4_32a *in_vel, const uint32_t *in_type, uint32_t T, const TreeBox &box,
-                 const double *mass_table, uint32_t ntypes, DevTree &tr, cudaStream_t s, cudaEvent_t after_sort);
+                 const double *mass_table, uint32_t ntypes, DevTree &tr, cudaStream_t s, cudaEvent_t after_sort, uint32_t leaf = 8);
 TreeBox make_box(const double center[3], double half_width);
 // Stage 2: densities, densest neighbours, HOP groups, clump stage -> host catalogue.
 int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogue **out);
+// --Density_Vs_Scale on the current tree (dvs.cu): the search radii and the densest sphere
+// of each, as BasicAnalysesWithTree reports them.
+int density_vs_scale(Context &c, const plan_params &p, double time, std::vector<double> &radii, std::vector<double> &rho, cudaStream_t s);
 // --Save_Clumps member lists of a catalogue, formatted on the device (parlist.cu).
 int write_parlists_device(Context &c, const plan_catalogue &cat, int file_number, uint32_t sampling, cudaStream_t s);
 // KNN queries at arbitrary positions on the current tree (inspection / tests).

@@ -80,3 +80,25 @@ def test_cli_device_member_lists(built, tmp_path):
                        timeout=300, env=env)
     assert r.returncode == 0, r.stderr
     assert cases.parlist_digests(out) == meta["parlist"]
+
+
+@pytest.mark.parametrize("name,case,extra", cases.DVS, ids=[v[0] for v in cases.DVS])
+def test_cli_density_vs_scale(name, case, extra, built, tmp_path):
+    """--Density_Vs_Scale through the drop-in binary: the RMPL file of sheared ball counts,
+    the clump finder on that run's tree (64-point leaves, no ghosts) and the reference's
+    routing of the basic results, every file byte for byte."""
+    g = GOLDEN / name
+    meta = json.loads((g / "meta.json").read_text())
+    m = cases.materialise(case, tmp_path / "in")
+    assert m["sha256"] == meta["lis_sha256"]
+    out = tmp_path / "out"
+    out.mkdir()
+    cli = ROOT / "plan_gb300" / "lib" / "plan_gpu"
+    r = subprocess.run([str(cli)] + cases.cli_args(m, str(out / "res.txt")) + extra, cwd=out, capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert [ln for ln in r.stdout.splitlines() if "Finish clump finding" in ln] == meta["summary"]
+    assert sorted(p.name for p in out.iterdir() if p.is_file()) == meta["files"]
+    for f in meta["files"]:
+        assert (out / f).read_bytes() == (g / f).read_bytes(), f
+    assert cases.parlist_digests(out) == meta["parlist"]

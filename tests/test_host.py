@@ -186,7 +186,7 @@ def test_cli_usage(built):
 
 def test_cli_rejects_what_is_not_on_this_path(built, tmp_path):
     base = ["-c", "1", "-i", str(tmp_path), "-b", "b", "-p", "p", "-f", "0:0", "-o", str(tmp_path / "o.txt"), "-t", "x"]
-    for extra in (["--Basic_Analyses"], ["--Density_Vs_Scale"], ["--Temp_Calculation"]):
+    for extra in (["--Basic_Analyses"], ["--Temp_Calculation"]):
         r = run_cli(base + extra)
         assert r.returncode == 2, extra
     r = run_cli(base + ["stray"])
