@@ -55,6 +55,10 @@ def lib() -> C.CDLL:
         L.orc_write_outputs.argtypes = [vp, C.c_char_p, C.c_int]
         L.orc_morton_order.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p]
         L.orc_set_user_box.argtypes = [vp, C.c_void_p, C.c_void_p]
+        L.orc_set_density_vs_scale.argtypes = [vp]
+        L.orc_density_vs_scale.restype = C.c_int
+        L.orc_density_vs_scale.argtypes = [vp, C.c_void_p, C.c_void_p, C.c_int]
+        L.orc_density_vs_scale_params.argtypes = [vp, C.c_void_p]
         _lib = L
     return _lib
 
@@ -70,7 +74,8 @@ def morton_order(keys3: np.ndarray) -> np.ndarray:
 class Oracle:
     """One snapshot through the CPU restatement: tree, densities, HOP, clumps."""
 
-    def __init__(self, lis, param: str | None, threads: int = 0, pow_mode: int = 0, no_ghost: bool = False, user_box=None):
+    def __init__(self, lis, param: str | None, threads: int = 0, pow_mode: int = 0, no_ghost: bool = False, user_box=None,
+                 density_vs_scale: bool = False):
         """lis: one path or the list of files of one snapshot (id0 first); user_box: optional
         ((lo_x, lo_y, lo_z), (hi_x, hi_y, hi_z)) as given by -x/-y/-z (0, 0 = unrestricted)."""
         L = lib()
@@ -81,10 +86,24 @@ class Oracle:
             lo = np.ascontiguousarray(user_box[0], dtype=np.float64)
             hi = np.ascontiguousarray(user_box[1], dtype=np.float64)
             L.orc_set_user_box(self._h, lo.ctypes.data, hi.ctypes.data)
+        if density_vs_scale:
+            L.orc_set_density_vs_scale(self._h)
         paths = [lis] if isinstance(lis, (str, bytes)) or not hasattr(lis, "__iter__") else list(lis)
         rc = L.orc_load(self._h, "\n".join(str(p) for p in paths).encode())
         if rc:
             raise RuntimeError(f"oracle: cannot read {lis} (status {rc})")
+
+    def density_vs_scale(self):
+        """BasicAnalysesWithTree on the loaded tree: (radii, densities)."""
+        r = np.zeros(32)
+        v = np.zeros(32)
+        n = lib().orc_density_vs_scale(self._h, r.ctypes.data, v.ctypes.data, 32)
+        return r[:n], v[:n]
+
+    def density_vs_scale_params(self) -> np.ndarray:
+        out = np.zeros(19)
+        lib().orc_density_vs_scale_params(self._h, out.ctypes.data)
+        return out
 
     def find(self) -> int:
         return int(lib().orc_find(self._h))

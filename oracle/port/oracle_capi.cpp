@@ -19,6 +19,7 @@ struct Ctx {
     double t_read = 0, t_tree = 0, t_find = 0;
     uint32_t n_input = 0;
     bool no_ghost = false;
+    bool dvs = false;  // --Density_Vs_Scale settings for the tree
 };
 double now() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -40,6 +41,39 @@ void *orc_open(const char *param_path, int threads, int pow_mode, int no_ghost) 
 }
 
 void orc_close(void *h) { delete static_cast<Ctx *>(h); }
+
+// --Density_Vs_Scale for the next orc_load: the tree as that analysis builds it (64-point
+// leaves, no ghosts, ghost zone as wide as the box; src/analyses.hpp:29-33)
+void orc_set_density_vs_scale(void *h) { static_cast<Ctx *>(h)->dvs = true; }
+
+// BasicAnalysesWithTree on the loaded tree: radii and densities; returns the number of radii
+int orc_density_vs_scale(void *h, double *radii, double *rho, int cap) {
+    Ctx *c = static_cast<Ctx *>(h);
+    DensityVsScale dv = density_vs_scale(c->finder.tree, c->par, c->snap.time);
+    for (int i = 0; i < (int)dv.radii.size() && i < cap; ++i) {
+        radii[i] = dv.radii[i];
+        rho[i] = dv.max_rhop[i];
+    }
+    return (int)dv.radii.size();
+}
+
+// The parameters the analysis reads: box_length[3], box_min[3], box_max[3], box_center[3],
+// box_half_width[0], max_half_width, cell_length[3], shear_speed, mass_per_particle[0], time
+void orc_density_vs_scale_params(void *h, double *out19) {
+    Ctx *c = static_cast<Ctx *>(h);
+    const Params &p = c->par;
+    for (int d = 0; d < 3; ++d) {
+        out19[d] = p.box_length[d];
+        out19[3 + d] = p.box_min[d];
+        out19[6 + d] = p.box_max[d];
+        out19[9 + d] = p.box_center[d];
+        out19[14 + d] = p.cell_length[d];
+    }
+    out19[12] = p.box_half_width[0];
+    out19[13] = p.max_half_width;
+    out19[17] = p.shear_speed;
+    out19[18] = p.mass_per_particle.empty() ? 0.0 : p.mass_per_particle[0];
+}
 
 // -x/-y/-z user box for the next orc_load (lo <= hi per axis; 0,0 = the box's extent)
 void orc_set_user_box(void *h, const double *lo3, const double *hi3) {
@@ -68,6 +102,11 @@ int orc_load(void *h, const char *lis_paths) {
     int rc = read_lis_files(files, c->snap);
     if (rc) return rc;
     finish_read(c->snap, c->par, true);
+    if (c->dvs) {
+        c->par.max_ghost_zone_width = c->par.max_half_width;
+        c->no_ghost = true;
+        c->finder.tree.max_leaf_size = 64;
+    }
     c->n_input = c->snap.num_particles;
     double t1 = now();
     if (!c->no_ghost) make_ghosts(c->snap, c->par);
