@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <vector>
 
+#include "octree_rules.cuh"
 #include "pipeline.h"
 #include "sort.h"
 
@@ -293,31 +294,17 @@ template <uint32_t LEAF>
 __global__ void k_lcp(const uint32_t *k0, const uint32_t *k1, const uint32_t *k2, uint32_t n, uint8_t *lcp_prev, uint8_t *win) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    int a = 0;
-    if (i > 0) a = key_lcp_digits(k0[i - 1], k1[i - 1], k2[i - 1], k0[i], k1[i], k2[i]);
-    lcp_prev[i] = (uint8_t)min(a, 31);
-    // (LEAF + 1)-key window starting at i: lcp of its first and last key
-    win[i] = (i + LEAF < n) ? (uint8_t)min(key_lcp_digits(k0[i], k1[i], k2[i], k0[i + LEAF], k1[i + LEAF], k2[i + LEAF]), 31)
-                            : (uint8_t)255;
+    lcp_prev[i] = octree_prev_lcp(k0, k1, k2, i);
+    win[i] = octree_window_lcp<LEAF>(k0, k1, k2, n, i);  // the (LEAF + 1)-key window starting at i
 }
 
-// leaf digit level: the node at digit level L containing i is internal iff some window of
-// LEAF + 1 consecutive keys containing i shares L digits (CountNodesLeaves' count > max_leaf_size
-// rule, src/tree.hpp:2674).
+// leaf digit level (CountNodesLeaves' count > max_leaf_size rule, src/tree.hpp:2674)
 template <uint32_t LEAF>
 __global__ void k_leaf_level(const uint8_t *win, uint32_t n, uint8_t *leaf_lvl) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    int M = 0;
-    uint32_t j0 = i >= LEAF ? i - LEAF : 0;
-    for (uint32_t j = j0; j <= i; ++j) {
-        uint8_t w = win[j];
-        if (w != 255 && w > M) M = w;
-    }
-    leaf_lvl[i] = (uint8_t)min(M + 1, 31);
+    leaf_lvl[i] = octree_leaf_level<LEAF>(win, i);
 }
-
-__device__ __forceinline__ bool starts_level(int L, int a, int l) { return L > a && L <= l; }
 
 __global__ void k_level_block_counts(const uint8_t *lcp_prev, const uint8_t *leaf_lvl, uint32_t n, uint32_t *bc /* [nb][32] */) {
     __shared__ uint32_t s[32];
