@@ -162,6 +162,18 @@ int plan_catalogue_basic_results(const plan_catalogue *cat, const plan_params *p
  * Writes up to cap values to radii and rho; *nlev = the number of radii. */
 int plan_density_vs_scale(plan_ctx *ctx, const plan_params *p, double time, double *radii, double *rho, int cap, int *nlev);
 
+/* Batched boundness (new, no counterpart in the reference): for each group g of particles
+ * [offsets[g], offsets[g+1]) (float32 positions, velocities, masses),
+ *   e_kin[g] = 1/2 sum m |v_c - s (x_c - x) - v|^2 with s = (0, q Omega, 0), the shear
+ *              correction of the reference's boundness test (src/tree.hpp:4657-4659), and
+ *   e_pot[g] = -G sum_{i<j} m_i m_j / r_ij (no softening; coincident pairs are left out and
+ *              counted in *zero_pairs).
+ * A group is bound when e_kin + e_pot < 0. All groups go through one persistent pass over
+ * 128 x 128 pair tiles; pair terms are FP32 with compensated sums, tile and group sums FP64.
+ * G, q and Omega come from p. */
+int plan_group_energies(plan_ctx *ctx, const float *pos3, const float *vel3, const float *mass, const uint64_t *offsets, uint32_t ngroups,
+                        const plan_params *p, double *e_kin, double *e_pot, uint64_t *zero_pairs);
+
 /* ---------------------------------------------------------------- serving
  * New, no counterpart in the reference (which processes its snapshot list one by one):
  * snapshots submitted from any thread run concurrently on one device, each on one of

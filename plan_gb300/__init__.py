@@ -111,6 +111,7 @@ def lib() -> C.CDLL:
             "plan_catalogue_write_peaks": (i32, [vp, C.c_char_p, i32, i32, u32]),
             "plan_catalogue_write_parlists": (i32, [vp, vp, i32, u32]),
             "plan_ctx_release": (i32, [vp]),
+            "plan_group_energies": (i32, [vp, vp, vp, vp, vp, u32, C.POINTER(Params), vp, vp, C.POINTER(C.c_uint64)]),
             "plan_server_create": (i32, [i32, i32, u64, C.POINTER(vp)]),
             "plan_server_destroy": (None, [vp]),
             "plan_submit": (i32, [vp, C.POINTER(LisView), C.POINTER(Params), i32, C.POINTER(C.c_uint64)]),
@@ -144,7 +145,7 @@ EXPORTED = [
     "plan_lis_time", "plan_lis_get_view", "plan_ctx_create", "plan_ctx_destroy", "plan_last_error", "plan_footprint_bytes",
     "plan_build_tree", "plan_find_planetesimals", "plan_find_clumps", "plan_catalogue_free", "plan_catalogue_count",
     "plan_catalogue_get", "plan_catalogue_summary", "plan_catalogue_write_peaks", "plan_catalogue_write_parlists",
-    "plan_catalogue_basic_results", "plan_ctx_release", "plan_server_create", "plan_server_destroy", "plan_submit", "plan_poll",
+    "plan_catalogue_basic_results", "plan_ctx_release", "plan_group_energies", "plan_server_create", "plan_server_destroy", "plan_submit", "plan_poll",
     "plan_server_error", "plan_server_stats",
     "plan_stage_count", "plan_stage_copy", "plan_knn", "plan_morton_order", "plan_morton_order_noalloc", "plan_stage_times", "plan_kernel_launches", "plan_counters",
     "plan_synth_default_spec", "plan_synth_records", "plan_synth_write_lis", "plan_synth_four_pi_G_for_mean",
@@ -333,6 +334,22 @@ class Finder:
         if rc:
             raise PlanError(rc, self.error())
         return out
+
+    def group_energies(self, pos, vel, mass, offsets, p: Params):
+        """Kinetic and potential energy of each group [offsets[g], offsets[g+1]) (float32 inputs);
+        returns (e_kin, e_pot, coincident pairs left out)."""
+        pos = np.ascontiguousarray(pos, dtype=np.float32)
+        vel = np.ascontiguousarray(vel, dtype=np.float32)
+        mass = np.ascontiguousarray(mass, dtype=np.float32)
+        off = np.ascontiguousarray(offsets, dtype=np.uint64)
+        ng = len(off) - 1
+        ek, ep = np.zeros(ng), np.zeros(ng)
+        z = C.c_uint64()
+        rc = lib().plan_group_energies(self._h, pos.ctypes.data, vel.ctypes.data, mass.ctypes.data, off.ctypes.data, ng, C.byref(p),
+                                       ek.ctypes.data, ep.ctypes.data, C.byref(z))
+        if rc:
+            raise PlanError(rc, self.error())
+        return ek, ep, int(z.value)
 
     def write_parlists(self, cat: "Catalogue", file_number: int = 0, sampling: int = 1) -> None:
         """The --Save_Clumps member lists of cat (ParList.<NNNN>/ in the working directory),

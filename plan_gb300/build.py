@@ -23,7 +23,7 @@ OUT = PKG / "lib"
 OBJ = PKG / "_build"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["radix_sort.cu", "scan.cu", "introsort.cu", "front.cu", "knn.cu", "hop.cu", "clumps.cu", "dvs.cu", "parlist.cu", "server.cu", "capi.cu"]
+CU_SOURCES = ["radix_sort.cu", "scan.cu", "introsort.cu", "front.cu", "knn.cu", "hop.cu", "clumps.cu", "dvs.cu", "energy.cu", "parlist.cu", "server.cu", "capi.cu"]
 HOST_SOURCES = ["host/params.cpp", "host/lis.cpp", "host/catalogue.cpp", "host/synth.cpp"]
 
 

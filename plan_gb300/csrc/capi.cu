@@ -397,6 +397,19 @@ int plan_density_vs_scale(plan_ctx *h, const plan_params *p, double time, double
     return c.status_from(rc, "plan_density_vs_scale");
 }
 
+int plan_group_energies(plan_ctx *h, const float *pos3, const float *vel3, const float *mass, const uint64_t *offsets, uint32_t ngroups,
+                        const plan_params *p, double *e_kin, double *e_pot, uint64_t *zero_pairs) {
+    if (!h || !p || !offsets || (ngroups && (!e_kin || !e_pot))) return kErrArgument;
+    if (ngroups && offsets[ngroups] && (!pos3 || !vel3 || !mass)) return kErrArgument;
+    Context &c = h->c;
+    g_ctx = &c;
+    c.last_error.clear();
+    cudaSetDevice(c.device);
+    const int rc = group_energies(c, pos3, vel3, mass, offsets, ngroups, p->grav_constant, p->q * p->Omega, e_kin, e_pot, zero_pairs,
+                                  c.stream);
+    return c.status_from(rc, "plan_group_energies");
+}
+
 int plan_catalogue_write_parlists(plan_ctx *h, const plan_catalogue *cat, int file_number, uint32_t sampling) {
     if (!h || !cat) return kErrArgument;
     Context &c = h->c;

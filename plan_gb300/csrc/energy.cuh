@@ -1,0 +1,61 @@
+// The pair-tile arithmetic of the batched boundness pass, host+device (energy.cu runs it on
+// the GPU; the CPU tests run the same functions over whole groups against an FP64 sum).
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+
+#ifdef __CUDACC__
+#define PLAN_EN_HD __host__ __device__
+#else
+#define PLAN_EN_HD
+#endif
+
+namespace plan {
+
+constexpr int kPairTile = 128;
+
+// Tile (ti, tj), tj >= ti, of the upper triangle of a T x T tiling, with tiles numbered row
+// by row: row ti starts at ti T - ti (ti - 1) / 2.
+PLAN_EN_HD inline uint64_t tri_row_start(uint64_t T, uint64_t k) { return k * T - k * (k - 1) / 2; }
+
+PLAN_EN_HD inline void tile_of(uint64_t local, uint64_t T, uint64_t &ti, uint64_t &tj) {
+    const double a = 2.0 * (double)T + 1.0;
+    const double r = std::floor((a - std::sqrt(a * a - 8.0 * (double)local)) / 2.0);
+    uint64_t t = r < 0 ? 0 : (uint64_t)r;
+    if (t >= T) t = T - 1;
+    while (t > 0 && tri_row_start(T, t) > local) --t;
+    while (t + 1 < T && tri_row_start(T, t + 1) <= local) ++t;
+    ti = t;
+    tj = t + (local - tri_row_start(T, t));
+}
+
+struct PairParticle {
+    float x, y, z, m;
+};
+
+// One row particle p against the columns col[0, cn) of its tile: sum of m_p m_q / r in FP32
+// with Neumaier's compensation (the returned pair is sum, compensation). Columns k <= skip_to
+// are left out (a diagonal tile: each pair once); coincident pairs are left out and counted.
+PLAN_EN_HD inline void pair_row_sum(const PairParticle &p, const PairParticle *col, uint32_t cn, int skip_to, float &sum, float &comp,
+                                    uint32_t &zeros) {
+    float s = 0.f, c = 0.f;
+    for (uint32_t k = 0; k < cn; ++k) {
+        if ((int)k <= skip_to) continue;
+        const PairParticle q = col[k];
+        const float dx = p.x - q.x, dy = p.y - q.y, dz = p.z - q.z;
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        if (d2 == 0.f) {
+            ++zeros;
+            continue;
+        }
+        const float term = p.m * q.m / std::sqrt(d2);
+        const float t = s + term;
+        c += std::fabs(s) >= std::fabs(term) ? (s - t) + term : (term - t) + s;
+        s = t;
+    }
+    sum = s;
+    comp = c;
+}
+
+}  // namespace plan

@@ -107,6 +107,9 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
 // --Density_Vs_Scale on the current tree (dvs.cu): the search radii and the densest sphere
 // of each, as BasicAnalysesWithTree reports them.
 int density_vs_scale(Context &c, const plan_params &p, double time, std::vector<double> &radii, std::vector<double> &rho, cudaStream_t s);
+// Kinetic and pairwise potential energy of particle groups (energy.cu).
+int group_energies(Context &c, const float *pos3, const float *vel3, const float *mass, const uint64_t *offsets, uint32_t ngroups, double G,
+                   double shear_y, double *e_kin, double *e_pot, uint64_t *zero_pairs, cudaStream_t s);
 // --Save_Clumps member lists of a catalogue, formatted on the device (parlist.cu).
 int write_parlists_device(Context &c, const plan_catalogue &cat, int file_number, uint32_t sampling, cudaStream_t s);
 // KNN queries at arbitrary positions on the current tree (inspection / tests).

@@ -1,9 +1,14 @@
-"""The serving loop on the GPU (needs a GB300): plan_submit / plan_poll.
+"""Workloads beyond one snapshot at a time, on the GPU (needs a GB300).
 
-Snapshots of different sizes are submitted together from several threads and run
-concurrently on a pool of contexts; each catalogue must equal the reference's golden output
-for that snapshot, i.e. be the same in the mix as alone. A tight budget forces requests to
-wait for memory and idle workers to give their buffers back; the results do not change.
+The serving loop (plan_submit / plan_poll): snapshots of different sizes are submitted
+together from several threads and run concurrently on a pool of contexts; each catalogue
+must equal the reference's golden output for that snapshot, i.e. be the same in the mix as
+alone. A tight budget forces requests to wait for memory and idle workers to give their
+buffers back; the results do not change.
+
+Batched boundness (plan_group_energies): kinetic and pairwise potential energies of groups
+from two to several thousand particles in one pass, against an FP64 direct sum (potential to
+1e-6 relative, the stated tolerance).
 """
 from __future__ import annotations
 
@@ -82,3 +87,36 @@ def test_oversized_request_is_refused(built, case_dir):
     finally:
         srv.close()
         snap.close()
+
+
+def test_group_energies_against_fp64(built):
+    import numpy as np
+
+    from test_energy_host import fp64_potential_sum, plummer_group
+
+    pg = built
+    sizes = [2, 31, 128, 129, 500, 2000, 3000, 64]
+    parts = [plummer_group(n, 100 + n) for n in sizes]
+    pos = np.concatenate([q[0] for q in parts])
+    vel = np.concatenate([q[1] for q in parts])
+    mass = np.concatenate([q[2] for q in parts])
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64)
+    p = pg.params()
+    pg.lib().plan_params_derive(__import__("ctypes").byref(p))
+    f = pg.Finder(0)
+    try:
+        ek, ep, zeros = f.group_energies(pos, vel, mass, off, p)
+    finally:
+        f.close()
+    assert zeros == 0
+    G, s = p.grav_constant, p.q * p.Omega
+    for g, (gp, gv, gm) in enumerate(parts):
+        want_p = -G * fp64_potential_sum(gp, gm)
+        assert abs(ep[g] - want_p) <= 1e-6 * abs(want_p), g
+        x, v, m = gp.astype(np.float64), gv.astype(np.float64), gm.astype(np.float64)
+        M = m.sum()
+        xc, vc = (m[:, None] * x).sum(0) / M, (m[:, None] * v).sum(0) / M
+        dv = vc[None, :] - v
+        dv[:, 1] -= s * (xc[0] - x[:, 0])
+        want_k = 0.5 * float((m * (dv ** 2).sum(1)).sum())
+        assert abs(ek[g] - want_k) <= 1e-12 * abs(want_k), g
