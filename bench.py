@@ -438,6 +438,60 @@ def run_serve(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- boundness (opt-in: --boundness K)
+def plummer_groups(k: int, n_lo: int, n_hi: int, seed: int):
+    """K Plummer groups (scale 1e-3, equal masses, float32), sizes log-uniform in [n_lo, n_hi]."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(n_lo), np.log(n_hi), k)).astype(np.int64)
+    pos, vel = [], []
+    for i, n in enumerate(sizes):
+        u = rng.uniform(1e-6, 0.99, n)
+        r = 1e-3 / np.sqrt(u ** (-2.0 / 3.0) - 1.0)
+        d = rng.normal(size=(n, 3))
+        d /= np.linalg.norm(d, axis=1)[:, None]
+        c = rng.uniform(-0.09, 0.09, 3)
+        pos.append((c + r[:, None] * d).astype(np.float32))
+        vel.append(rng.normal(scale=1e-3, size=(n, 3)).astype(np.float32))
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64)
+    return np.concatenate(pos), np.concatenate(vel), np.full(int(off[-1]), 4.0106053e-08, np.float32), off
+
+
+def run_boundness(args) -> None:
+    """All groups' energies through plan_group_energies; pair interactions per second."""
+    import torch
+
+    import plan_gb300 as pg
+
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py: no CUDA device (this path has no CPU fallback)")
+    pos, vel, mass, off = plummer_groups(args.boundness, 32, args.boundness_max, SEED)
+    sizes = np.diff(off.astype(np.int64))
+    pairs = int((sizes * (sizes - 1) // 2).sum())
+    p = pg.params()
+    pg.lib().plan_params_derive(C.byref(p))
+    f = pg.Finder(0)
+    for _ in range(args.warmup):
+        f.group_energies(pos, vel, mass, off, p)
+    clocks = ClockSampler(0)
+    clocks.start()
+    t = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        ek, ep, zeros = f.group_energies(pos, vel, mass, off, p)
+        t.append(time.perf_counter() - t0)
+    clk = clocks.stop()
+    f.close()
+    sec = sum(t) / len(t)
+    line = {"metric": "pair interactions/s (batched boundness)", "value": pairs / sec, "unit": "pairs/s", "n_gpus": 1,
+            "higher_is_better": True, "data": "synthetic", "dtype": "f32 pairs, f64 sums", "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * sec,
+            "config": {"workload": f"{args.boundness} Plummer groups, sizes log-uniform in [32, {args.boundness_max}]",
+                       "particles": int(off[-1]), "pairs": pairs, "bound_groups": int((ek + ep < 0).sum()), "coincident_pairs": zeros},
+            "e2e": {"value": pairs / sec, "unit": "pairs/s", "h2d_bytes_per_step": int(off[-1]) * 28, "d2h_bytes_per_step": 16 * len(sizes)},
+            "clocks": clk}
+    print(json.dumps(line), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -451,8 +505,12 @@ def main() -> None:
     ap.add_argument("--serve-workers", type=int, default=3)
     ap.add_argument("--serve-rate", type=float, default=4.0, help="Poisson arrivals per second")
     ap.add_argument("--serve-max-log2", type=int, default=22, help="largest request 2^k particles")
+    ap.add_argument("--boundness", type=int, default=0, help="instead: K groups through plan_group_energies")
+    ap.add_argument("--boundness-max", type=int, default=200000, help="largest group")
     args = ap.parse_args()
-    if args.serve and args.impl == "gpu":
+    if args.boundness and args.impl == "gpu":
+        run_boundness(args)
+    elif args.serve and args.impl == "gpu":
         run_serve(args)
     elif args.impl == "reference":
         run_reference(args)

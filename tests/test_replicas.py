@@ -5,6 +5,7 @@ from __future__ import annotations
 import os
 import socket
 
+import numpy as np
 import pytest
 import torch.multiprocessing as mp
 
@@ -69,3 +70,14 @@ def test_serving_requests_and_latency_stats():
     assert len({sd for _, sd in a}) == 64
     st = bench.latency_stats([1.0, 2.0, 3.0, 4.0])
     assert st["p50"] == 2.5 and st["n"] == 4 and 3.9 < st["p99"] <= 4.0
+
+
+def test_boundness_groups():
+    """The boundness leg's groups: sizes log-uniform in range, offsets consistent, float32."""
+    import bench
+
+    pos, vel, mass, off = bench.plummer_groups(20, 32, 2000, 1)
+    sizes = np.diff(off.astype(np.int64))
+    assert len(sizes) == 20 and sizes.min() >= 32 and sizes.max() <= 2000
+    assert pos.shape == (int(off[-1]), 3) and vel.shape == pos.shape and mass.shape == (int(off[-1]),)
+    assert pos.dtype == np.float32 and mass.dtype == np.float32
