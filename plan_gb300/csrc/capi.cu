@@ -372,8 +372,8 @@ int plan_density_vs_scale(plan_ctx *h, const plan_params *p, double time, double
     g_ctx = &c;
     c.last_error.clear();
     cudaSetDevice(c.device);
-    if (!c.tree.Tu) {
-        c.last_error = "plan_density_vs_scale: no tree (call plan_build_tree first)";
+    if (!c.tree.Tu || c.tree.leaf_size != 64) {
+        c.last_error = "plan_density_vs_scale: no tree built for it (plan_build_tree with density_vs_scale set)";
         return kErrArgument;
     }
     std::vector<double> r, v;

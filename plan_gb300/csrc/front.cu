@@ -532,6 +532,7 @@ int build_octree(Context &c, double4_32a *in_pos, double4_32a *in_vel, const uin
                                                    tr.tk1, tr.tk2, tr.sink_n, tr.sink_first);
     c.launches++;
     tr.nsinks = T - Tu;
+    tr.leaf_size = leaf;
 
     // octree (src/tree.hpp:2848-2886)
     uint8_t *lcp_prev = S.get<uint8_t>(Tu), *win = S.get<uint8_t>(Tu), *leaf_lvl = S.get<uint8_t>(Tu);

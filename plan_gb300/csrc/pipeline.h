@@ -48,6 +48,7 @@ struct TreeBox {
 
 struct DevTree {
     uint32_t T = 0, Tu = 0, nodes = 0, nsinks = 0;
+    uint32_t leaf_size = 8;  // max_leaf_size it was built with (64 for --Density_Vs_Scale)
     TreeBox box;
     double4_32a *pos = nullptr, *vel = nullptr;
     double *dens = nullptr;
