@@ -1164,7 +1164,7 @@ __global__ void __launch_bounds__(kRebindThreads) k_rebind_round(const uint32_t 
             tf[i] = cf;
         }
         __syncthreads();
-        if (kSpec && threadIdx.x < 32) {
+        if (kSpec == 1 && threadIdx.x < 32) {
             // Speculative windows, exact by verification: decide 32 candidates against the
             // window's first state, run the FP64 update chain through the tentative
             // acceptances only, then check every decision against the exact state before it.
@@ -1292,7 +1292,9 @@ __global__ void __launch_bounds__(kRebindThreads) k_rebind_round(const uint32_t 
                 ++iters;
                 const uint32_t k = at + lane;
                 bool bound = false;
+                double yk = 0;  // kSpec == 2: 1 / (M + m_k), taken while the lanes test
                 if (k < tend && !ttaken[k - base]) {
+                    if (kSpec == 2) yk = 1.0 / (M_ + tpos[k - base].w);
                     const int r = bound_hilo(tf[k - base], Mf, sh, sl, G32, shear32);
                     bound = r >= 0 ? r == 1 : bound_fp64(tpos[k - base], tvel[k - base], M_, x_, y_, z_, vx_, vy_, vz_, cp);
                 }
@@ -1313,7 +1315,17 @@ __global__ void __launch_bounds__(kRebindThreads) k_rebind_round(const uint32_t 
                     const int c = lane < 6 ? lane : 0;
                     const double sc = c == 0 ? x_ : c == 1 ? y_ : c == 2 ? z_ : c == 3 ? vx_ : c == 4 ? vy_ : vz_;
                     const double qc = c == 0 ? p.x : c == 1 ? p.y : c == 2 ? p.z : c == 3 ? v.x : c == 4 ? v.y : v.z;
-                    const double r = (sc * M + p.w * qc) / M;
+                    double r;
+                    if (kSpec == 2) {
+                        // the correctly rounded quotient from the reciprocal the accepted lane
+                        // took (Markstein's correction, as in the speculative windows)
+                        const double yr = __shfl_sync(0xffffffffu, yk, f);
+                        const double num = sc * M + p.w * qc;
+                        const double q0 = num * yr;
+                        r = num == 0.0 ? num : fma(fma(-q0, M, num), yr, q0);
+                    } else {
+                        r = (sc * M + p.w * qc) / M;
+                    }
                     float rh, rl;
                     split_f(r, rh, rl);
                     for (int q = 0; q < 6; ++q) {
@@ -2275,7 +2287,10 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
         // speculative acceptance windows (exact by verification; PLAN_ACCEPT_SPECULATE=1)
         const char *spec_env = std::getenv("PLAN_ACCEPT_SPECULATE");
         const bool speculate = spec_env && *spec_env == '1';
-        auto rebind_kernel = speculate ? k_rebind_round<1> : k_rebind_round<0>;
+        // the default loop with the reciprocal taken during the test (PLAN_ACCEPT_RCP=1)
+        const char *rcp_env = std::getenv("PLAN_ACCEPT_RCP");
+        const bool rcp = rcp_env && *rcp_env == '1';
+        auto rebind_kernel = speculate ? k_rebind_round<1> : rcp ? k_rebind_round<2> : k_rebind_round<0>;
         uint64_t rounds = 0, passes = 0, reruns = 0;
         // Rounds until no clump grows. Clumps in `waiting` start once every clump listed as
         // their blocker has finished (reruns in key order where their balls may meet).
