@@ -178,6 +178,21 @@ def test_large_snapshot_against_oracle(n, seed, pg, finder, tmp_path):
     thousands of members take the large-clump paths (ordered sums over warps, the radix sort
     of member distances, concurrent Hill rebinding with reruns). The catalogue must equal the
     oracle's byte for byte, and densities and densest pointers bit for bit."""
+    check_large_snapshot(n, seed, pg, finder, tmp_path)
+
+
+@pytest.mark.skipif(os.environ.get("PLAN_TEST_ACCEPT_VARIANTS") != "1",
+                    reason="opt-in acceptance loops; run with PLAN_TEST_ACCEPT_VARIANTS=1")
+@pytest.mark.parametrize("switch", ["PLAN_ACCEPT_SPECULATE", "PLAN_ACCEPT_RCP"])
+@pytest.mark.parametrize("n,seed", [(1 << 20, 2), (1 << 21, 4)])
+def test_large_snapshot_acceptance_variants(switch, n, seed, pg, finder, tmp_path, monkeypatch):
+    """The opt-in Hill-rebinding acceptance loops (speculative windows; the reciprocal taken
+    during the test) must give the same catalogue as the oracle on the large snapshots."""
+    monkeypatch.setenv(switch, "1")
+    check_large_snapshot(n, seed, pg, finder, tmp_path)
+
+
+def check_large_snapshot(n, seed, pg, finder, tmp_path):
     import oracle
 
     c = cases.Case(f"w2_{n}", 2, n, seed, 128)
