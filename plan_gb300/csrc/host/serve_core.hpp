@@ -123,8 +123,10 @@ class ServeQueue {
     int workers() const { return (int)held_.size(); }
 
    private:
-    // Start what can start; called with the lock held.
+    // Start what can start; called with the lock held. Nothing starts once shutting down (a
+    // worker that has left its loop would never run it).
     void schedule_locked() {
+        if (stop_) return;
         bool started = true;
         while (started && !queue_.empty()) {
             started = false;
