@@ -144,6 +144,35 @@ def multi_snapshot() -> None:
         print("multi_snapshot:", *summary, sep="\n  ")
 
 
+def multi_density_vs_scale() -> None:
+    """The two-snapshot run with --Density_Vs_Scale alone: one RMPL header, a line per
+    snapshot, the basic results in the same file, the summary stream scientific throughout."""
+    with tempfile.TemporaryDirectory() as tmp:
+        tmp = Path(tmp)
+        d = tmp / "in"
+        d.mkdir()
+        for k, c in enumerate(cases.MULTI):
+            m = cases.materialise(c, tmp / f"c{k}")
+            shutil.copy(m["lis"][0], d / f"Snap.{k:04d}.ds.lis")
+            if k == 0:
+                shutil.copy(m["param"], d / "para.txt")
+        out = tmp / "ref"
+        out.mkdir()
+        args = ["-c", "1", "-i", str(d), "-b", "Snap", "-p", "ds", "-f", "0:1", "-o", str(out / "res.txt"), "-t", str(d / "para.txt"),
+                "--Combined", "--Density_Vs_Scale"]
+        r = subprocess.run([str(REF)] + args, cwd=out, capture_output=True, text=True, check=True)
+        g = HERE / "multi_density_vs_scale"
+        if g.exists():
+            shutil.rmtree(g)
+        g.mkdir()
+        files = sorted(p.name for p in out.iterdir() if p.is_file())
+        for f in files:
+            shutil.copy(out / f, g / f)
+        summary = [ln for ln in r.stdout.splitlines() if "Finish clump finding" in ln]
+        (g / "meta.json").write_text(json.dumps({"summary": summary, "files": files}, indent=1) + "\n")
+        print("multi_density_vs_scale:", files, *summary, sep="\n  ")
+
+
 def variants() -> None:
     """Command-line and parameter variants of one snapshot, run by the reference's CLI."""
     for name, c, extra in cases.VARIANTS:
@@ -202,6 +231,7 @@ def main() -> None:
         variants()
     if not only or "dvs" in only:
         dvs_variants()
+        multi_density_vs_scale()
     for c in cases.CASES + cases.SPLINE:
         if only and c.name not in only:
             continue

@@ -102,3 +102,23 @@ def test_cli_density_vs_scale(name, case, extra, built, tmp_path):
     for f in meta["files"]:
         assert (out / f).read_bytes() == (g / f).read_bytes(), f
     assert cases.parlist_digests(out) == meta["parlist"]
+
+
+def test_cli_two_snapshots_density_vs_scale(built, tmp_path):
+    """The drop-in binary over two snapshots with --Density_Vs_Scale alone writes the
+    reference's files (one RMPL header, lines and basic results interleaved)."""
+    from test_oracle_golden import _multi_inputs, multi_snapshot_args
+
+    g = GOLDEN / "multi_density_vs_scale"
+    meta = json.loads((g / "meta.json").read_text())
+    d, _ = _multi_inputs(tmp_path)
+    out = tmp_path / "out"
+    out.mkdir()
+    cli = ROOT / "plan_gb300" / "lib" / "plan_gpu"
+    r = subprocess.run([str(cli)] + multi_snapshot_args(d, out) + ["--Density_Vs_Scale"], cwd=out, capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stderr
+    assert [ln for ln in r.stdout.splitlines() if "Finish clump finding" in ln] == meta["summary"]
+    assert sorted(p.name for p in out.iterdir() if p.is_file()) == meta["files"]
+    for f in meta["files"]:
+        assert (out / f).read_bytes() == (g / f).read_bytes(), f

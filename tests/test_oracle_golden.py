@@ -181,3 +181,22 @@ def test_oracle_cli_density_vs_scale(name, case, extra, oracle_mod, tmp_path):
     for f in meta["files"]:
         assert (out / f).read_bytes() == (g / f).read_bytes(), f
     assert cases.parlist_digests(out) == meta["parlist"]
+
+
+def test_oracle_cli_two_snapshots_density_vs_scale(oracle_mod, tmp_path):
+    """Two snapshots with --Density_Vs_Scale alone: one RMPL header, then per snapshot its
+    line followed by the basic results, and scientific summary lines throughout."""
+    import json
+    import subprocess
+
+    g = GOLDEN / "multi_density_vs_scale"
+    meta = json.loads((g / "meta.json").read_text())
+    d, _ = _multi_inputs(tmp_path)
+    out = tmp_path / "out"
+    out.mkdir()
+    r = subprocess.run([str(oracle_mod.CLI)] + multi_snapshot_args(d, out) + ["--Density_Vs_Scale"], cwd=out, capture_output=True,
+                       text=True, check=True)
+    assert [ln for ln in r.stdout.splitlines() if "Finish clump finding" in ln] == meta["summary"]
+    assert sorted(p.name for p in out.iterdir() if p.is_file()) == meta["files"]
+    for f in meta["files"]:
+        assert (out / f).read_bytes() == (g / f).read_bytes(), f
