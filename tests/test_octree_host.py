@@ -81,7 +81,7 @@ def oracle_mod(built):
 
 
 def _by_case(name):
-    for c in cases.CASES:
+    for c in cases.CASES + cases.SPLINE:
         if c.name == name:
             return c, False
     for v in cases.DVS:
@@ -90,7 +90,7 @@ def _by_case(name):
     raise KeyError(name)
 
 
-@pytest.mark.parametrize("name", ["w1_20k", "w1_20k_sinks", "w1_20k_sheared", "w1_24k_split2", "w1_20k_dvs16", "w1_20k_dvs32_sheared"])
+@pytest.mark.parametrize("name", [c.name for c in cases.CASES + cases.SPLINE] + [v[0] for v in cases.DVS[::2]])
 def test_octree_rules_give_the_oracle_nodes(name, shim, oracle_mod, tmp_path):
     case, dvs = _by_case(name)
     m = cases.materialise(case, tmp_path / "in")
