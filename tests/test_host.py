@@ -76,6 +76,22 @@ def test_struct_layouts_match_the_header(built, tmp_path):
             assert int(got[f"{st}.{n}"]) == getattr(cls, n).offset, (st, n)
 
 
+def test_headers_are_plain_c(built, tmp_path):
+    """The boundary is usable from C: both headers compile as C99 with every warning, and a C
+    program links against the library and calls it (parameter defaults, no device needed)."""
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    (tmp_path / "c.c").write_text(
+        '#include "plan_gpu.h"\n#include "plan_synth.h"\n#include <stdio.h>\n'
+        "int main(void) { plan_params p; plan_params_init(&p); printf(\"%u %u %d\\n\", p.knn, p.hop, (int)p.user_box); return 0; }\n")
+    lib = ROOT / "plan_gb300" / "lib"
+    subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", str(ROOT / "include"), str(tmp_path / "c.c"),
+                    f"-L{lib}", "-lplan_gpu", f"-Wl,-rpath,{lib}", "-o", str(tmp_path / "c")], check=True)
+    out = subprocess.run([str(tmp_path / "c")], capture_output=True, text=True, check=True).stdout.split()
+    assert out == ["64", "32", "0"]
+
+
 # ---------------------------------------------------------------- parameters
 def test_params_defaults(built):
     p = built.params()
