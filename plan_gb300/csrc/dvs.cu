@@ -95,8 +95,10 @@ int density_vs_scale(Context &c, const plan_params &p, double time, std::vector<
     dp.mass_per_particle0 = p.mass_per_particle[0];
     DvsGeom g;
     std::vector<double> xs, ys, zs;
-    if (dvs_setup(dp, time, key_to_double(ext[0]), key_to_double(ext[1]), g, xs, ys, zs)) {
-        c.last_error = "density vs scale: the grid gives more radii than supported";
+    const int src = dvs_setup(dp, time, key_to_double(ext[0]), key_to_double(ext[1]), g, xs, ys, zs);
+    if (src) {
+        c.last_error = src == -1 ? "density vs scale: the grid gives more radii than supported"
+                                 : "density vs scale: the points or the box need more than 2^24 cell centres along an axis";
         return kErrUnsupported;
     }
     std::vector<uint32_t> maxc(g.nlev, 0);

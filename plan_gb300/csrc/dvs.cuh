@@ -45,8 +45,10 @@ struct DvsParams {
 };
 
 // Geometry and cell-centre coordinates, with the reference's host arithmetic (the centres are
-// accumulated x += cell as its loops do). zlo, zhi: extreme z of the tree points. 0, or -1
-// when the grid gives more radii than kDvsMaxLevels.
+// accumulated x += cell as its loops do). zlo, zhi: extreme z of the tree points. 0; -1 when
+// the grid gives more radii than kDvsMaxLevels; -2 when an axis would need more than 2^24
+// centres (coordinates far outside any box the parameters describe, where the reference's
+// loops would run for ever).
 inline int dvs_setup(const DvsParams &p, double time, double zlo, double zhi, DvsGeom &g, std::vector<double> &xs, std::vector<double> &ys,
                      std::vector<double> &zs) {
     g = DvsGeom{};
@@ -59,6 +61,11 @@ inline int dvs_setup(const DvsParams &p, double time, double zlo, double zhi, Dv
     }
     g.shear = p.shear_speed * time;
     g.diag = std::sqrt(3);
+    const double kMaxCentres = 16777216.0;
+    if (!(p.cell_length[0] > 0 && p.cell_length[1] > 0 && p.cell_length[2] > 0)) return -2;
+    for (int d = 0; d < 2; ++d)
+        if (!((p.box_max[d] - p.box_min[d]) / p.cell_length[d] < kMaxCentres)) return -2;
+    if (!((zhi - zlo) / p.cell_length[2] < kMaxCentres) || !(std::fabs(p.box_center[2] - zlo) / p.cell_length[2] < kMaxCentres)) return -2;
     double z_min = p.box_center[2] - p.cell_length[2] / 2.0;
     const double z_max = zhi;
     while (z_min - p.cell_length[2] > zlo) z_min -= p.cell_length[2];
