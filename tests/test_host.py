@@ -217,3 +217,18 @@ def test_cli_parameter_file_errors_before_device(built, tmp_path):
             str(tmp_path / "missing.txt"), "--Combined"]
     r = run_cli(base)
     assert r.returncode == 3
+
+
+def test_no_device_no_fallback(built):
+    """Without a CUDA device every device entry point fails with status 5: the context, the
+    serving loop, and so every computation behind them. There is no CPU path to fall back on."""
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    with pytest.raises(built.PlanError) as e:
+        built.Finder(0)
+    assert e.value.status == 5
+    with pytest.raises(built.PlanError) as e:
+        built.Server(0, 2, 0)
+    assert e.value.status == 5
