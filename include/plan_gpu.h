@@ -169,7 +169,8 @@ int plan_density_vs_scale(plan_ctx *ctx, const plan_params *p, double time, doub
  *   e_pot[g] = -G sum_{i<j} m_i m_j / r_ij (no softening; coincident pairs are left out and
  *              counted in *zero_pairs).
  * A group is bound when e_kin + e_pot < 0. All groups go through one persistent pass over
- * 128 x 128 pair tiles; pair terms are FP32 with compensated sums, tile and group sums FP64.
+ * 128 x 128 pair tiles; row sums of m_j / r_ij are FP32 with compensation, the mass of the
+ * row, the tile and group sums FP64.
  * G, q and Omega come from p. */
 int plan_group_energies(plan_ctx *ctx, const float *pos3, const float *vel3, const float *mass, const uint64_t *offsets, uint32_t ngroups,
                         const plan_params *p, double *e_kin, double *e_pot, uint64_t *zero_pairs);

@@ -11,9 +11,9 @@
 // part: every group is cut into 128 x 128 tiles of pairs (the upper triangle, diagonal tiles
 // included) and a persistent grid of blocks takes tiles from one queue across all groups, so
 // groups from tens to millions of particles share the GPU without a launch per size. A tile
-// stages its 128 column particles in shared memory; each thread sums its row's terms in FP32
-// with compensated (Neumaier) addition; the block adds the threads' sums in FP64 and one FP64
-// atomic per tile adds that to the group. Coincident pairs (r = 0) are left out and counted.
+// stages its 128 column particles in shared memory; each thread sums its row's m_j / r_ij in
+// FP32 with compensated (Neumaier) addition and multiplies by its m_i in FP64; the block adds
+// the threads' sums in FP64 and one FP64 atomic per tile adds that to the group. Coincident pairs (r = 0) are left out and counted.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -105,12 +105,14 @@ __global__ void __launch_bounds__(kPairTile) k_pair_potential(const float4 *pm, 
         __syncthreads();
         float s = 0.f, comp = 0.f;
         uint32_t zeros = 0;
+        double mrow = 0;
         if (r < n) {
             const float4 q = pm[b + r];
             const uint32_t cn = (uint32_t)(n - c0 < (uint64_t)kPairTile ? n - c0 : (uint64_t)kPairTile);
             pair_row_sum(PairParticle{q.x, q.y, q.z, q.w}, col, cn, ti == tj ? (int)threadIdx.x : -1, s, comp, zeros);
+            mrow = q.w;
         }
-        red[threadIdx.x] = (double)s + (double)comp;
+        red[threadIdx.x] = mrow * ((double)s + (double)comp);
         if (zeros) atomicAdd(zero_pairs, (unsigned long long)zeros);
         __syncthreads();
         for (int h = kPairTile / 2; h > 0; h >>= 1) {

@@ -34,9 +34,11 @@ struct PairParticle {
     float x, y, z, m;
 };
 
-// One row particle p against the columns col[0, cn) of its tile: sum of m_p m_q / r in FP32
-// with Neumaier's compensation (the returned pair is sum, compensation). Columns k <= skip_to
-// are left out (a diagonal tile: each pair once); coincident pairs are left out and counted.
+// One row particle p against the columns col[0, cn) of its tile: sum of m_q / r in FP32 with
+// Neumaier's compensation (the returned pair is sum, compensation); the caller multiplies by
+// m_p in FP64, so no pair's mass product is rounded in FP32 (equal masses would otherwise
+// round every term the same way). Columns k <= skip_to are left out (a diagonal tile: each
+// pair once); coincident pairs are left out and counted.
 PLAN_EN_HD inline void pair_row_sum(const PairParticle &p, const PairParticle *col, uint32_t cn, int skip_to, float &sum, float &comp,
                                     uint32_t &zeros) {
     float s = 0.f, c = 0.f;
@@ -49,7 +51,7 @@ PLAN_EN_HD inline void pair_row_sum(const PairParticle &p, const PairParticle *c
             ++zeros;
             continue;
         }
-        const float term = p.m * q.m / std::sqrt(d2);
+        const float term = q.m / std::sqrt(d2);
         const float t = s + term;
         c += std::fabs(s) >= std::fabs(term) ? (s - t) + term : (term - t) + s;
         s = t;

@@ -54,11 +54,13 @@ extern "C" double pair_sum_host(const float *pos3, const float *mass, uint64_t n
             const uint64_t r = ti * kPairTile + t;
             float s = 0.f, c = 0.f;
             uint32_t z = 0;
+            double mrow = 0;
             if (r < n) {
                 const uint32_t cn = (uint32_t)(n - c0 < (uint64_t)kPairTile ? n - c0 : (uint64_t)kPairTile);
                 pair_row_sum(PairParticle{pos3[3 * r], pos3[3 * r + 1], pos3[3 * r + 2], mass[r]}, col.data(), cn, ti == tj ? t : -1, s, c, z);
+                mrow = mass[r];
             }
-            red[t] = (double)s + (double)c;
+            red[t] = mrow * ((double)s + (double)c);
             zeros += z;
         }
         for (int h = kPairTile / 2; h > 0; h >>= 1)
