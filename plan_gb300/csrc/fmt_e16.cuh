@@ -16,6 +16,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cstring>
 
 #ifdef __CUDACC__
 #define PLAN_FMT_HD __host__ __device__
@@ -180,14 +181,7 @@ PLAN_FMT_HD inline void fmt_e16_w24(double v, char *out) {
     char buf[24];
     int len = 0;
     uint64_t bits;
-    {
-        union {
-            double d;
-            uint64_t u;
-        } cvt;
-        cvt.d = v;
-        bits = cvt.u;
-    }
+    memcpy(&bits, &v, sizeof bits);
     const bool neg = (bits >> 63) != 0;
     const int bexp = (int)((bits >> 52) & 0x7ff);
     const uint64_t frac = bits & 0xfffffffffffffull;
