@@ -101,6 +101,12 @@ int density_vs_scale(Context &c, const plan_params &p, double time, std::vector<
                                  : "density vs scale: the points or the box need more than 2^24 cell centres along an axis";
         return kErrUnsupported;
     }
+    // one thread per query: at most 2^31 - 1 blocks of 128 (each axis is below 2^24, so the
+    // product is checked in double before it is formed in 64 bits)
+    if ((double)g.nx * g.ny * g.nz * g.nvar > 2147483647.0 * 128.0) {
+        c.last_error = "density vs scale: the grid has more queries than one launch can take";
+        return kErrUnsupported;
+    }
     std::vector<uint32_t> maxc(g.nlev, 0);
     const uint64_t nthreads = (uint64_t)g.nx * g.ny * g.nz * g.nvar;
     if (nthreads) {
