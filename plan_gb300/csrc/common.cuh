@@ -31,6 +31,21 @@ enum Status : int {
 
 int set_cuda_error(cudaError_t e, const char *what, const char *file, int line);
 
+// A stream-ordered device allocation, freed on its stream when it leaves scope (so an early
+// return on an error does not leak it).
+template <class T>
+struct StreamBuf {
+    T *p = nullptr;
+    cudaStream_t s;
+    explicit StreamBuf(cudaStream_t st) : s(st) {}
+    StreamBuf(const StreamBuf &) = delete;
+    StreamBuf &operator=(const StreamBuf &) = delete;
+    ~StreamBuf() {
+        if (p) cudaFreeAsync(p, s);
+    }
+    cudaError_t alloc(size_t count) { return cudaMallocAsync(reinterpret_cast<void **>(&p), (count ? count : 1) * sizeof(T), s); }
+};
+
 // ------------------------------------------------------------------ device error flags
 // Kernels never trap: a bounded loop that runs out, or an index that would leave its
 // buffer, sets a bit here and returns; the host checks after the stage.

@@ -71,16 +71,16 @@ int density_vs_scale(Context &c, const plan_params &p, double time, std::vector<
     const DevTree &tr = c.tree;
     if (!tr.Tu || !tr.pos) return kErrArgument;
     // z extent of the tree points (RecursiveFindExtreme finds the extreme values exactly)
-    unsigned long long *d_ext = nullptr;
-    PLAN_CUDA(cudaMallocAsync(&d_ext, 16, s));
+    StreamBuf<unsigned long long> d_ext(s);
+    PLAN_CUDA(d_ext.alloc(2));
     const unsigned long long init[2] = {~0ull, 0ull};
-    PLAN_CUDA(cudaMemcpyAsync(d_ext, init, 16, cudaMemcpyHostToDevice, s));
-    k_z_extent<<<grid_for(tr.Tu, 256), 256, 0, s>>>(tr.pos, tr.Tu, d_ext);
+    PLAN_CUDA(cudaMemcpyAsync(d_ext.p, init, 16, cudaMemcpyHostToDevice, s));
+    k_z_extent<<<grid_for(tr.Tu, 256), 256, 0, s>>>(tr.pos, tr.Tu, d_ext.p);
     c.launches++;
+    PLAN_CUDA(cudaGetLastError());
     unsigned long long ext[2];
-    PLAN_CUDA(cudaMemcpyAsync(ext, d_ext, 16, cudaMemcpyDeviceToHost, s));
+    PLAN_CUDA(cudaMemcpyAsync(ext, d_ext.p, 16, cudaMemcpyDeviceToHost, s));
     PLAN_CUDA(cudaStreamSynchronize(s));
-    PLAN_CUDA(cudaFreeAsync(d_ext, s));
     DvsParams dp;
     for (int d = 0; d < 3; ++d) {
         dp.box_length[d] = p.box_length[d];
@@ -110,25 +110,21 @@ int density_vs_scale(Context &c, const plan_params &p, double time, std::vector<
     std::vector<uint32_t> maxc(g.nlev, 0);
     const uint64_t nthreads = (uint64_t)g.nx * g.ny * g.nz * g.nvar;
     if (nthreads) {
-        double *d_x = nullptr, *d_y = nullptr, *d_z = nullptr;
-        uint32_t *d_max = nullptr;
-        PLAN_CUDA(cudaMallocAsync(&d_x, xs.size() * 8, s));
-        PLAN_CUDA(cudaMallocAsync(&d_y, ys.size() * 8, s));
-        PLAN_CUDA(cudaMallocAsync(&d_z, zs.size() * 8, s));
-        PLAN_CUDA(cudaMallocAsync(&d_max, (size_t)g.nlev * 4, s));
-        PLAN_CUDA(cudaMemcpyAsync(d_x, xs.data(), xs.size() * 8, cudaMemcpyHostToDevice, s));
-        PLAN_CUDA(cudaMemcpyAsync(d_y, ys.data(), ys.size() * 8, cudaMemcpyHostToDevice, s));
-        PLAN_CUDA(cudaMemcpyAsync(d_z, zs.data(), zs.size() * 8, cudaMemcpyHostToDevice, s));
-        PLAN_CUDA(cudaMemsetAsync(d_max, 0, (size_t)g.nlev * 4, s));
-        k_dvs<<<(unsigned)((nthreads + 127) / 128), 128, 0, s>>>(DevTreeView{ktree_of(tr)}, d_x, d_y, d_z, g, d_max, c.d_err);
+        StreamBuf<double> d_x(s), d_y(s), d_z(s);
+        StreamBuf<uint32_t> d_max(s);
+        PLAN_CUDA(d_x.alloc(xs.size()));
+        PLAN_CUDA(d_y.alloc(ys.size()));
+        PLAN_CUDA(d_z.alloc(zs.size()));
+        PLAN_CUDA(d_max.alloc(g.nlev));
+        PLAN_CUDA(cudaMemcpyAsync(d_x.p, xs.data(), xs.size() * 8, cudaMemcpyHostToDevice, s));
+        PLAN_CUDA(cudaMemcpyAsync(d_y.p, ys.data(), ys.size() * 8, cudaMemcpyHostToDevice, s));
+        PLAN_CUDA(cudaMemcpyAsync(d_z.p, zs.data(), zs.size() * 8, cudaMemcpyHostToDevice, s));
+        PLAN_CUDA(cudaMemsetAsync(d_max.p, 0, (size_t)g.nlev * 4, s));
+        k_dvs<<<(unsigned)((nthreads + 127) / 128), 128, 0, s>>>(DevTreeView{ktree_of(tr)}, d_x.p, d_y.p, d_z.p, g, d_max.p, c.d_err);
         c.launches++;
         PLAN_CUDA(cudaGetLastError());
-        PLAN_CUDA(cudaMemcpyAsync(maxc.data(), d_max, (size_t)g.nlev * 4, cudaMemcpyDeviceToHost, s));
+        PLAN_CUDA(cudaMemcpyAsync(maxc.data(), d_max.p, (size_t)g.nlev * 4, cudaMemcpyDeviceToHost, s));
         PLAN_CUDA(cudaStreamSynchronize(s));
-        cudaFreeAsync(d_x, s);
-        cudaFreeAsync(d_y, s);
-        cudaFreeAsync(d_z, s);
-        cudaFreeAsync(d_max, s);
     }
     radii.assign(g.radius, g.radius + g.nlev);
     rho.resize(g.nlev);

@@ -142,50 +142,41 @@ int group_energies(Context &c, const float *pos3, const float *vel3, const float
         hpm[i] = make_float4(pos3[3 * i], pos3[3 * i + 1], pos3[3 * i + 2], mass[i]);
         hv[i] = make_float4(vel3[3 * i], vel3[3 * i + 1], vel3[3 * i + 2], 0.f);
     }
-    float4 *d_pm = nullptr, *d_v = nullptr;
-    uint64_t *d_off = nullptr, *d_items = nullptr;
-    double *d_ek = nullptr, *d_sum = nullptr;
-    double4_32a *d_com = nullptr;
-    unsigned long long *d_next = nullptr;
-    PLAN_CUDA(cudaMallocAsync(&d_pm, (n ? n : 1) * sizeof(float4), s));
-    PLAN_CUDA(cudaMallocAsync(&d_v, (n ? n : 1) * sizeof(float4), s));
-    PLAN_CUDA(cudaMallocAsync(&d_off, (ngroups + 1) * 8, s));
-    PLAN_CUDA(cudaMallocAsync(&d_items, (ngroups + 1) * 8, s));
-    PLAN_CUDA(cudaMallocAsync(&d_ek, ngroups * 8, s));
-    PLAN_CUDA(cudaMallocAsync(&d_sum, ngroups * 8, s));
-    PLAN_CUDA(cudaMallocAsync(&d_com, ngroups * sizeof(double4_32a), s));
-    PLAN_CUDA(cudaMallocAsync(&d_next, 16, s));
-    PLAN_CUDA(cudaMemcpyAsync(d_pm, hpm.data(), n * sizeof(float4), cudaMemcpyHostToDevice, s));
-    PLAN_CUDA(cudaMemcpyAsync(d_v, hv.data(), n * sizeof(float4), cudaMemcpyHostToDevice, s));
-    PLAN_CUDA(cudaMemcpyAsync(d_off, offsets, (ngroups + 1) * 8, cudaMemcpyHostToDevice, s));
-    PLAN_CUDA(cudaMemcpyAsync(d_items, item_off.data(), (ngroups + 1) * 8, cudaMemcpyHostToDevice, s));
-    PLAN_CUDA(cudaMemsetAsync(d_sum, 0, ngroups * 8, s));
-    PLAN_CUDA(cudaMemsetAsync(d_next, 0, 16, s));
-    k_group_kinetic<<<ngroups, 256, 0, s>>>(d_pm, d_v, d_off, ngroups, shear_y, d_ek, d_com);
+    StreamBuf<float4> d_pm(s), d_v(s);
+    StreamBuf<uint64_t> d_off(s), d_items(s);
+    StreamBuf<double> d_ek(s), d_sum(s);
+    StreamBuf<double4_32a> d_com(s);
+    StreamBuf<unsigned long long> d_next(s);  // [0] the tile queue, [1] coincident pairs
+    PLAN_CUDA(d_pm.alloc(n));
+    PLAN_CUDA(d_v.alloc(n));
+    PLAN_CUDA(d_off.alloc(ngroups + 1));
+    PLAN_CUDA(d_items.alloc(ngroups + 1));
+    PLAN_CUDA(d_ek.alloc(ngroups));
+    PLAN_CUDA(d_sum.alloc(ngroups));
+    PLAN_CUDA(d_com.alloc(ngroups));
+    PLAN_CUDA(d_next.alloc(2));
+    PLAN_CUDA(cudaMemcpyAsync(d_pm.p, hpm.data(), n * sizeof(float4), cudaMemcpyHostToDevice, s));
+    PLAN_CUDA(cudaMemcpyAsync(d_v.p, hv.data(), n * sizeof(float4), cudaMemcpyHostToDevice, s));
+    PLAN_CUDA(cudaMemcpyAsync(d_off.p, offsets, (ngroups + 1) * 8, cudaMemcpyHostToDevice, s));
+    PLAN_CUDA(cudaMemcpyAsync(d_items.p, item_off.data(), (ngroups + 1) * 8, cudaMemcpyHostToDevice, s));
+    PLAN_CUDA(cudaMemsetAsync(d_sum.p, 0, ngroups * 8, s));
+    PLAN_CUDA(cudaMemsetAsync(d_next.p, 0, 16, s));
+    k_group_kinetic<<<ngroups, 256, 0, s>>>(d_pm.p, d_v.p, d_off.p, ngroups, shear_y, d_ek.p, d_com.p);
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const unsigned grid = (unsigned)std::min<uint64_t>((uint64_t)sms * 8, nitems ? nitems : 1);
-    k_pair_potential<<<grid, kPairTile, 0, s>>>(d_pm, d_off, d_items, ngroups, nitems, d_next, d_sum, d_next + 1);
+    k_pair_potential<<<grid, kPairTile, 0, s>>>(d_pm.p, d_off.p, d_items.p, ngroups, nitems, d_next.p, d_sum.p, d_next.p + 1);
     c.launches += 2;
     PLAN_CUDA(cudaGetLastError());
     std::vector<double> sum(ngroups);
     unsigned long long zeros = 0;
-    PLAN_CUDA(cudaMemcpyAsync(e_kin, d_ek, ngroups * 8, cudaMemcpyDeviceToHost, s));
-    PLAN_CUDA(cudaMemcpyAsync(sum.data(), d_sum, ngroups * 8, cudaMemcpyDeviceToHost, s));
-    PLAN_CUDA(cudaMemcpyAsync(&zeros, d_next + 1, 8, cudaMemcpyDeviceToHost, s));
+    PLAN_CUDA(cudaMemcpyAsync(e_kin, d_ek.p, ngroups * 8, cudaMemcpyDeviceToHost, s));
+    PLAN_CUDA(cudaMemcpyAsync(sum.data(), d_sum.p, ngroups * 8, cudaMemcpyDeviceToHost, s));
+    PLAN_CUDA(cudaMemcpyAsync(&zeros, d_next.p + 1, 8, cudaMemcpyDeviceToHost, s));
     PLAN_CUDA(cudaStreamSynchronize(s));
     for (uint32_t g = 0; g < ngroups; ++g) e_pot[g] = -G * sum[g];
     if (zero_pairs) *zero_pairs = zeros;
-    cudaFreeAsync(d_pm, s);
-    cudaFreeAsync(d_v, s);
-    cudaFreeAsync(d_off, s);
-    cudaFreeAsync(d_items, s);
-    cudaFreeAsync(d_ek, s);
-    cudaFreeAsync(d_sum, s);
-    cudaFreeAsync(d_com, s);
-    cudaFreeAsync(d_next, s);
-    PLAN_CUDA(cudaStreamSynchronize(s));
     return kOk;
 }
 
