@@ -106,7 +106,10 @@ class Oracle:
         return out
 
     def find(self) -> int:
-        return int(lib().orc_find(self._h))
+        n = int(lib().orc_find(self._h))
+        if n < 0:
+            raise ValueError(f"oracle: {self.summary()}")
+        return n
 
     def timings(self) -> np.ndarray:
         a = np.zeros(3)

@@ -13,6 +13,7 @@
 #include <limits>
 #include <numeric>
 #include <sstream>
+#include <stdexcept>
 #include <sys/stat.h>
 
 #ifdef _OPENMP
@@ -1012,6 +1013,11 @@ std::string Finder::find(uint32_t num_in) {
     peaks_and_masses.clear();
     stats = Stats();
     const uint32_t T = tree.size();
+    // KNN_Search_OpenMP asserts knn <= num_particles (src/tree.hpp:3199). The reference is
+    // built with NDEBUG, and then its radius-doubling loop never ends on such a snapshot: the
+    // restatement refuses it, as the device path does.
+    if (p.knn < 1 || p.hop < 1 || p.knn > T || p.hop > T)
+        throw std::domain_error("knn and hop must be at least 1 and not exceed the number of tree points");
     // kernel choice, src/tree.hpp:3576-3611
     uint32_t horiz = p.box_resolution[0] * p.box_resolution[1];
     if (tree.half_width < p.max_half_width + p.max_ghost_zone_width - 1e-16)

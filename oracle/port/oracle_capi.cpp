@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cstring>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -102,6 +103,7 @@ int orc_load(void *h, const char *lis_paths) {
     int rc = read_lis_files(files, c->snap);
     if (rc) return rc;
     finish_read(c->snap, c->par, true);
+    if (c->snap.num_particles == 0) return 7;  // the reference has no check and crashes in BuildTree
     if (c->dvs) {
         c->par.max_ghost_zone_width = c->par.max_half_width;
         c->no_ghost = true;
@@ -121,7 +123,12 @@ int orc_load(void *h, const char *lis_paths) {
 int orc_find(void *h) {
     Ctx *c = static_cast<Ctx *>(h);
     double t0 = now();
-    c->summary = c->finder.find(c->n_input);
+    try {
+        c->summary = c->finder.find(c->n_input);
+    } catch (const std::domain_error &e) {
+        c->summary = e.what();
+        return -7;
+    }
     c->t_find = now() - t0;
     return (int)c->finder.num_planetesimals;
 }

@@ -8,6 +8,7 @@
 #include <getopt.h>
 #include <iomanip>
 #include <sstream>
+#include <stdexcept>
 #include <string>
 #include <utility>
 #include <vector>
@@ -123,6 +124,10 @@ int main(int argc, char **argv) {
         int rc = read_lis_files(files, snap);
         if (rc) return rc;
         finish_read(snap, par, first);
+        if (snap.num_particles == 0) {  // the reference has no check and crashes in BuildTree
+            std::fprintf(stderr, "Error: the snapshot holds no particles\n");
+            return 5;
+        }
         if (f_dvs) {  // BasicAnalyses' settings for --Density_Vs_Scale (src/analyses.hpp:29-33)
             par.max_ghost_zone_width = par.max_half_width;
             f_noghost = 1;
@@ -146,7 +151,13 @@ int main(int argc, char **argv) {
             std::fwrite(txt.data(), 1, txt.size(), rf);
         }
         double t2 = now();
-        std::string summary = f.find(nin);
+        std::string summary;
+        try {
+            summary = f.find(nin);
+        } catch (const std::domain_error &e) {
+            std::fprintf(stderr, "Error: %s\n", e.what());
+            return 5;
+        }
         double t3 = now();
         std::printf("%s\n", summary.c_str());
         write_peaks_file(peaks_file_name(out, snap.time), f);

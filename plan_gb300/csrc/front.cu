@@ -619,7 +619,11 @@ int build_tree(Context &c, const plan_lis_view &v, plan_params &p, int first_fil
     cudaEventRecord(ev[0], s);
     uint64_t N64 = 0;
     for (uint32_t b = 0; b < v.nblocks; ++b) N64 += v.counts[b];
-    if (N64 == 0 || N64 >= 0xfffffff0ull) return kErrUnsupported;
+    if (N64 == 0) {
+        c.last_error = "the snapshot holds no particles";
+        return kErrUnsupported;
+    }
+    if (N64 >= 0xfffffff0ull) return kErrUnsupported;
     uint32_t N = (uint32_t)N64;  // the particles that take part (after the user box)
     c.n_input = N;
     c.time = v.time;

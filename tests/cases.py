@@ -35,7 +35,7 @@ class Case:
     n: int
     seed: int
     nx: int
-    edit: str = ""          # "", "sinks", "border", "split2", "uniform"
+    edit: str = ""          # "", "sinks", "border", "split2", "uniform", "small:<nb>:<nc>"
     time: float = 0.0
     knn: int = 32
     hop: int = 16
@@ -60,7 +60,14 @@ SPLINE = [
     Case("w1_50k_spline", 1, 50000, 31, 128),
     Case("w1_20k_spline80", 1, 20000, 35, 80),
 ]
-BY_NAME = {c.name: c for c in CASES + SPLINE}
+# small snapshots cut from the 20k one (the first records, from the uniform background, and
+# the last ones, from the clumps): a few hundred particles with clumps among them
+SMALL = [
+    Case("w1_1k_small", 1, 20000, 5, 32, edit="small:100:900"),   # spline kernel, 4 clumps
+    Case("w1_1k_small8", 1, 20000, 5, 8, edit="small:600:400"),   # median kernel (N >= 4 Nx Ny)
+    Case("w1_200_small", 1, 20000, 5, 8, edit="small:60:140"),    # spline kernel, 1 clump
+]
+BY_NAME = {c.name: c for c in CASES + SPLINE + SMALL}
 # command-line and parameter variants of one snapshot: (name, case, extra arguments)
 VARIANTS = [
     ("w1_20k_parlist_s3", Case("w1_20k", 1, 20000, 5, 32), ["--Save_Clumps", "-s", "3"]),
@@ -137,6 +144,11 @@ def _edit(c: Case, rec: np.ndarray) -> list[np.ndarray]:
             x = np.where(x >= np.float32(0.1), (x - np.float32(0.2)).astype(np.float32), x)
             x = np.where(x < np.float32(-0.1), np.float32(-0.1), x)
             p[:, d] = x
+    elif c.edit.startswith("small:"):
+        # the first nb records and the last nc, renumbered
+        nb, nc = (int(v) for v in c.edit.split(":")[1:])
+        rec = np.concatenate([rec[:nb], rec[n - nc:]]).copy()
+        rec["id_in_run"] = np.arange(len(rec))
     elif c.edit == "uniform":
         # the background only: no clump should survive
         keep = n - n // 5

@@ -232,7 +232,7 @@ def main() -> None:
     if not only or "dvs" in only:
         dvs_variants()
         multi_density_vs_scale()
-    for c in cases.CASES + cases.SPLINE:
+    for c in cases.CASES + cases.SPLINE + cases.SMALL:
         if only and c.name not in only:
             continue
         with tempfile.TemporaryDirectory() as tmp:

@@ -80,8 +80,13 @@ def oracle_mod(built):
     return oracle
 
 
+# snapshots of 1 to 14 particles (with their ghosts): trees whose root is a leaf or has only
+# a few leaves, as the clump trees of the merge sweeps often are
+TINY = [cases.Case(f"tiny_{nb}_{nc}", 1, 20000, 5, 32, edit=f"small:{nb}:{nc}") for nb, nc in ((1, 0), (5, 0), (0, 8), (3, 6), (0, 14))]
+
+
 def _by_case(name):
-    for c in cases.CASES + cases.SPLINE:
+    for c in cases.CASES + cases.SPLINE + cases.SMALL + TINY:
         if c.name == name:
             return c, False
     for v in cases.DVS:
@@ -90,7 +95,7 @@ def _by_case(name):
     raise KeyError(name)
 
 
-@pytest.mark.parametrize("name", [c.name for c in cases.CASES + cases.SPLINE] + [v[0] for v in cases.DVS[::2]])
+@pytest.mark.parametrize("name", [c.name for c in cases.CASES + cases.SPLINE + cases.SMALL + TINY] + [v[0] for v in cases.DVS[::2]])
 def test_octree_rules_give_the_oracle_nodes(name, shim, oracle_mod, tmp_path):
     case, dvs = _by_case(name)
     m = cases.materialise(case, tmp_path / "in")

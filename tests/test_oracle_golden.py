@@ -14,7 +14,7 @@ import pytest
 import cases
 from conftest import GOLDEN, golden
 
-CPU_CASES = [c.name for c in cases.CASES + cases.SPLINE]
+CPU_CASES = [c.name for c in cases.CASES + cases.SPLINE + cases.SMALL]
 
 
 @pytest.fixture(scope="module")
@@ -135,6 +135,32 @@ def test_oracle_cli_two_snapshots(oracle_mod, tmp_path):
     for name in meta["peaks_files"]:
         assert (out / name).read_bytes() == (g / name).read_bytes()
     assert (out / "res_planetesimals.txt").read_bytes() == (g / "planetesimals.txt").read_bytes()
+
+
+@pytest.mark.parametrize("keep", [(0, 0), (20, 0)], ids=["empty", "20_particles"])
+def test_oracle_refuses_what_the_reference_cannot_finish(keep, oracle_mod, tmp_path):
+    """An empty snapshot, and one with fewer tree points than the neighbours asked for
+    (knn = 32). The reference crashes on the first (a segmentation fault here) and never
+    returns from the second: KNN_Search_OpenMP's assert is compiled out and its radius keeps
+    doubling (src/tree.hpp:3199-3237). The restatement refuses both with an error and exit
+    status 5, as the device path does (status 7 from the C ABI, exit status 5 from its CLI)."""
+    import subprocess
+
+    m = cases.materialise(cases.Case("refused", 1, 20000, 5, 32, edit="small:%d:%d" % keep), tmp_path / "in")
+    out = tmp_path / "out"
+    out.mkdir()
+    r = subprocess.run([str(oracle_mod.CLI)] + cases.cli_args(m, str(out / "res.txt")), cwd=out, capture_output=True, text=True,
+                       timeout=60)
+    assert r.returncode == 5
+    assert "Error:" in r.stderr
+    if keep == (0, 0):
+        with pytest.raises(RuntimeError):
+            oracle_mod.Oracle(m["lis"], m["param"], threads=1)
+    else:
+        o = oracle_mod.Oracle(m["lis"], m["param"], threads=1)
+        assert len(o.keys()) < 32
+        with pytest.raises(ValueError):
+            o.find()
 
 
 @pytest.mark.parametrize("name,case,extra", cases.VARIANTS, ids=[v[0] for v in cases.VARIANTS])
