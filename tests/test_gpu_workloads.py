@@ -13,6 +13,7 @@ from two to several thousand particles in one pass, against an FP64 direct sum (
 from __future__ import annotations
 
 import threading
+import time
 
 import pytest
 
@@ -33,6 +34,18 @@ def _check(pg, name, cat, tmp_path):
     d.mkdir()
     cat.write_peaks(str(d / "res.txt"))
     assert (d / g["peaks_file"]).read_bytes() == (GOLDEN / name / g["peaks_file"]).read_bytes(), name
+
+
+def _poll_until(srv, rid, seconds):
+    """Poll without blocking inside the library, so a request that never finishes fails the
+    test instead of holding it."""
+    end = time.monotonic() + seconds
+    while time.monotonic() < end:
+        got = srv.poll(rid)
+        if got is not None:
+            return got
+        time.sleep(0.01)
+    return None
 
 
 @pytest.mark.parametrize("workers,budget_of_largest", [(3, 0.0), (2, 1.2)])
@@ -63,8 +76,8 @@ def test_mixed_requests_match_alone(workers, budget_of_largest, built, case_dir,
             t.join()
         assert len(ids) == len(MIX)
         for n in MIX:
-            got = srv.poll(ids[n], wait=True)
-            assert got is not None
+            got = _poll_until(srv, ids[n], 600.0)
+            assert got is not None, f"request {n} not done after 600 s"
             cat, lat = got
             assert lat > 0
             _check(pg, n, cat, tmp_path / f"w{workers}")
