@@ -902,10 +902,108 @@ void Finder::remove_unbound(Clump &c) const {  // src/tree.hpp:4615-4674
     sort_particles(c);
 }
 
+// Replays one call's candidates three ways with the reference's own test and update: in
+// sequence; as the device's default loop steps (each step tests the next 32 candidates and
+// takes the first bound one); and as speculative windows (all 32 decided against the
+// window's first state, the state chained through those tentative acceptances, each decision
+// checked against the state before it, the agreeing prefix kept and the first disagreeing
+// candidate decided exactly). Counts the steps of each; the speculative result must equal the
+// sequential one.
+void Finder::count_windows(const Clump &c, const std::vector<uint32_t> &near) {
+    struct St {
+        double M;
+        V3 com, vcom;
+    };
+    const Params &p = *par;
+    std::vector<uint32_t> E;
+    for (uint32_t idx : near)
+        if (!tree.pts[idx].in_clump_flag && tree.pts[idx].new_density >= density_threshold) E.push_back(idx);
+    auto bound = [&](const St &s, uint32_t idx) {
+        const TreePoint &t = tree.pts[idx];
+        double M = s.M + t.mass;
+        V3 dv = sub(sub(s.vcom, mul(p.shear_vector, s.com[0] - t.pos[0])), t.vel);
+        return +0.5 / M * norm2(dv) - p.grav_constant / norm(sub(s.com, t.pos)) < 0;
+    };
+    auto update = [&](St &s, uint32_t idx) {
+        const TreePoint &t = tree.pts[idx];
+        s.M = s.M + t.mass;
+        s.com = div(add(mul(s.com, s.M), mul(t.mass, t.pos)), s.M);
+        s.vcom = div(add(mul(s.M, s.vcom), mul(t.mass, t.vel)), s.M);
+    };
+    const St s0{c.total_mass, c.center_of_mass, c.vel_com};
+    const size_t n = E.size();
+    std::vector<size_t> seq, spec;
+    St s = s0;
+    for (size_t k = 0; k < n; ++k)
+        if (bound(s, E[k])) {
+            update(s, E[k]);
+            seq.push_back(k);
+        }
+    uint64_t first_bound = 0;
+    s = s0;
+    for (size_t at = 0; at < n; ++first_bound) {
+        const size_t end = std::min(at + 32, n);
+        size_t j = end;
+        for (size_t k = at; k < end && j == end; ++k)
+            if (bound(s, E[k])) j = k;
+        if (j < end) update(s, E[j]);
+        at = j < end ? j + 1 : end;
+    }
+    uint64_t windows = 0;
+    s = s0;
+    for (size_t at = 0; at < n; ++windows) {
+        const int w = (int)(std::min(at + 32, n) - at);
+        bool tent[32];
+        St chain[33];
+        chain[0] = s;
+        int nt = 0;
+        for (int l = 0; l < w; ++l) {
+            tent[l] = bound(s, E[at + l]);
+            if (tent[l]) {
+                chain[nt + 1] = chain[nt];
+                update(chain[nt + 1], E[at + l]);
+                ++nt;
+            }
+        }
+        int below = 0, m = -1, kept = 0;
+        for (int l = 0; l < w && m < 0; ++l) {
+            if (bound(chain[below], E[at + l]) != tent[l]) m = l;
+            else if (tent[l]) {
+                spec.push_back(at + l);
+                ++below;
+                ++kept;
+            }
+        }
+        s = chain[below];
+        if (m >= 0) {
+            ++window_stats.mismatch_windows;
+            if (!tent[m]) {  // the exact state binds it
+                update(s, E[at + m]);
+                spec.push_back(at + m);
+                ++kept;
+            }
+            at += (size_t)m + 1;
+        } else {
+            at += (size_t)w;
+        }
+        ++window_stats.accepted_per_window[kept];
+    }
+    WindowStats &ws = window_stats;
+    ws.calls++;
+    ws.candidates += n;
+    ws.accepted += seq.size();
+    ws.first_bound_steps += first_bound;
+    ws.first_bound_max = std::max(ws.first_bound_max, first_bound);
+    ws.speculative_steps += windows;
+    ws.speculative_max = std::max(ws.speculative_max, windows);
+    if (spec != seq) ws.disagreements++;
+}
+
 void Finder::search_bound_in_hill(Clump &c) {  // src/tree.hpp:4678-4711
     const Params &p = *par;
     std::vector<uint32_t> near;
     tree.ball(c.center_of_mass, c.Hill_radius, near);
+    if (window_stats_on) count_windows(c, near);
     for (uint32_t idx : near) {
         TreePoint &t = tree.pts[idx];
         if (t.in_clump_flag || t.new_density < density_threshold) continue;

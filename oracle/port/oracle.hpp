@@ -197,6 +197,17 @@ struct Stats {
     uint64_t zero_key_quirk = 0;
 };
 
+// Acceptance-window statistics of the Hill rebinding (a study mode, PLAN_ORACLE_WINDOW_STATS=1):
+// each call's candidate sequence replayed with 32-candidate windows, the way the device's
+// default acceptance loop and its speculative windows step through it.
+struct WindowStats {
+    uint64_t calls = 0, candidates = 0, accepted = 0;
+    uint64_t first_bound_steps = 0, first_bound_max = 0;      // test 32, take the first bound one, restart after it
+    uint64_t speculative_steps = 0, speculative_max = 0;      // decide 32 against one state, verify, keep the agreeing prefix
+    uint64_t mismatch_windows = 0, disagreements = 0;         // windows cut short; calls whose result differed (must be 0)
+    uint64_t accepted_per_window[33] = {0};
+};
+
 struct Finder {
     Params *par = nullptr;
     Tree tree;
@@ -232,6 +243,9 @@ struct Finder {
     void merge(Clump &pred, Clump &prey) const;
     void remove_unbound(Clump &c) const;
     void search_bound_in_hill(Clump &c);
+    bool window_stats_on = false;
+    WindowStats window_stats;
+    void count_windows(const Clump &c, const std::vector<uint32_t> &near);
     void hill(Clump &c) const;
     void angular_momentum(Clump &c) const;
     bool bound(const Clump &a, const Clump &b) const;

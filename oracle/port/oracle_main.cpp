@@ -142,6 +142,7 @@ int main(int argc, char **argv) {
         f.time = snap.time;
         // the shared summary stream is left scientific by an earlier snapshot's basic results
         // or by this snapshot's density-vs-scale lines
+        f.window_stats_on = std::getenv("PLAN_ORACLE_WINDOW_STATS") != nullptr;
         f.stream_scientific = !first || f_dvs;
         if (f_dvs) f.tree.max_leaf_size = 64;
         f.tree.build(par, snap.parts, true);
@@ -160,6 +161,17 @@ int main(int argc, char **argv) {
         }
         double t3 = now();
         std::printf("%s\n", summary.c_str());
+        if (f.window_stats_on) {
+            const WindowStats &w = f.window_stats;
+            std::fprintf(stderr,
+                         "[oracle] Hill rebinding: %llu calls, %llu candidates, %llu accepted; first-bound steps %llu (longest call %llu); "
+                         "speculative windows %llu (longest call %llu), %llu cut short, %llu calls disagreeing\n[oracle] accepted per window:",
+                         (unsigned long long)w.calls, (unsigned long long)w.candidates, (unsigned long long)w.accepted,
+                         (unsigned long long)w.first_bound_steps, (unsigned long long)w.first_bound_max, (unsigned long long)w.speculative_steps,
+                         (unsigned long long)w.speculative_max, (unsigned long long)w.mismatch_windows, (unsigned long long)w.disagreements);
+            for (uint64_t v : w.accepted_per_window) std::fprintf(stderr, " %llu", (unsigned long long)v);
+            std::fprintf(stderr, "\n");
+        }
         write_peaks_file(peaks_file_name(out, snap.time), f);
         if (f_save) {
             std::ostringstream sid;

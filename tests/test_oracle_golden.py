@@ -137,6 +137,34 @@ def test_oracle_cli_two_snapshots(oracle_mod, tmp_path):
     assert (out / "res_planetesimals.txt").read_bytes() == (g / "planetesimals.txt").read_bytes()
 
 
+@pytest.mark.parametrize("name", ["w1_20k", "w1_20k_sinks", "w2_250k", "config1_262k"])
+def test_speculative_windows_replay_the_sequential_loop(name, case_dir, oracle_mod, tmp_path):
+    """The device's speculative acceptance windows (PLAN_ACCEPT_SPECULATE) in the reference's
+    own Hill rebinding: every call's candidates replayed in 32-candidate windows decided
+    against one state, checked against the exact state before each, and cut at the first
+    disagreement, accept exactly what the sequential loop accepts, in fewer steps than the
+    default loop's one acceptance per step. The run's files stay the reference's."""
+    import re
+    import subprocess
+
+    g = golden(name)
+    m = case_dir(name)
+    out = tmp_path / "out"
+    out.mkdir()
+    env = dict(os.environ, PLAN_ORACLE_WINDOW_STATS="1")
+    r = subprocess.run([str(oracle_mod.CLI)] + cases.cli_args(m, str(out / "res.txt")), cwd=out, env=env, capture_output=True, text=True,
+                       check=True)
+    assert g["summary"] in r.stdout
+    assert (out / "res_planetesimals.txt").read_bytes() == (GOLDEN / name / "planetesimals.txt").read_bytes()
+    st = re.search(r"(\d+) calls, (\d+) candidates, (\d+) accepted; first-bound steps (\d+) \(longest call \d+\); "
+                   r"speculative windows (\d+) \(longest call \d+\), (\d+) cut short, (\d+) calls disagreeing", r.stderr)
+    assert st, r.stderr
+    calls, cands, acc, first_bound, windows, cut, disagree = map(int, st.groups())
+    assert calls > 0 and acc > 0
+    assert disagree == 0
+    assert windows <= first_bound
+
+
 @pytest.mark.parametrize("keep", [(0, 0), (20, 0)], ids=["empty", "20_particles"])
 def test_oracle_refuses_what_the_reference_cannot_finish(keep, oracle_mod, tmp_path):
     """An empty snapshot, and one with fewer tree points than the neighbours asked for
