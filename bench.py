@@ -163,8 +163,9 @@ def write_lis(path: Path, rec: np.ndarray, n: int) -> None:
 
 
 # ---------------------------------------------------------------- CPU legs
-def cpu_sample(n: int, seed: int, threads: int, reps: int = 1) -> dict:
-    """The oracle restatement on a sample snapshot of the same workload: particles/s."""
+def cpu_sample(n: int, seed: int, threads: int, reps: int = 1, warmup: int = 0) -> dict:
+    """The oracle restatement on a sample snapshot of the same workload, generated once:
+    `warmup` untimed passes, then the seconds of `reps` timed ones (read to catalogue)."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle
 
@@ -174,11 +175,12 @@ def cpu_sample(n: int, seed: int, threads: int, reps: int = 1) -> dict:
         write_lis(d / "Snap.0000.ds.lis", rec.numpy(), n)
         write_params(d / "para.txt", fourpig, threads)
         times = []
-        for _ in range(reps):
+        for k in range(warmup + reps):
             t0 = time.perf_counter()
             o = oracle.Oracle(str(d / "Snap.0000.ds.lis"), str(d / "para.txt"), threads=threads, pow_mode=0)
             o.find()
-            times.append(time.perf_counter() - t0)
+            if k >= warmup:
+                times.append(time.perf_counter() - t0)
             o.close()
     return {"n": n, "seconds": times}
 
@@ -193,9 +195,7 @@ def run_reference(args) -> None:
     b.build_oracle()
     threads = os.cpu_count() or 1
     n = args.sample_n
-    for _ in range(args.warmup):
-        cpu_sample(n, SEED, threads)
-    r = cpu_sample(n, SEED, threads, reps=args.steps)
+    r = cpu_sample(n, SEED, threads, reps=args.steps, warmup=args.warmup)
     per = [n / t for t in r["seconds"]]
     value = args.steps * n / sum(r["seconds"])
     sample = f"{n} particles of the same workload (same mixture and clump mass function, clump count scaled), {args.steps} snapshots"
