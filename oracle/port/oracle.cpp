@@ -902,13 +902,18 @@ void Finder::remove_unbound(Clump &c) const {  // src/tree.hpp:4615-4674
     sort_particles(c);
 }
 
-// Replays one call's candidates three ways with the reference's own test and update: in
-// sequence; as the device's default loop steps (each step tests the next 32 candidates and
-// takes the first bound one); and as speculative windows (all 32 decided against the
-// window's first state, the state chained through those tentative acceptances, each decision
-// checked against the state before it, the agreeing prefix kept and the first disagreeing
-// candidate decided exactly). Counts the steps of each; the speculative result must equal the
-// sequential one.
+// Replays one call's candidates with the reference's own test and update, in sequence and
+// in five ways of stepping through them, and counts the steps of each (a step being what one
+// pass of a warp or block does before the state may change):
+//   0, 1, 2  first bound: test the next 32, 256 or 1024 candidates against the state, take the
+//            first bound one (or none) and continue after it;
+//   3        speculative windows of 32: all decided against the window's first state, the
+//            state chained through those tentative acceptances, each decision checked against
+//            the state before it, the agreeing prefix kept and the first disagreeing candidate
+//            decided exactly;
+//   4        as 3, but a 256-wide scan first skips to the next candidate bound under the
+//            current state, so a stretch without any bound candidate costs one step.
+// The speculative results must equal the sequential one.
 void Finder::count_windows(const Clump &c, const std::vector<uint32_t> &near) {
     struct St {
         double M;
@@ -932,33 +937,36 @@ void Finder::count_windows(const Clump &c, const std::vector<uint32_t> &near) {
     };
     const St s0{c.total_mass, c.center_of_mass, c.vel_com};
     const size_t n = E.size();
-    std::vector<size_t> seq, spec;
+    std::vector<size_t> seq;
     St s = s0;
     for (size_t k = 0; k < n; ++k)
         if (bound(s, E[k])) {
             update(s, E[k]);
             seq.push_back(k);
         }
-    uint64_t first_bound = 0;
-    s = s0;
-    for (size_t at = 0; at < n; ++first_bound) {
-        const size_t end = std::min(at + 32, n);
-        size_t j = end;
-        for (size_t k = at; k < end && j == end; ++k)
-            if (bound(s, E[k])) j = k;
-        if (j < end) update(s, E[j]);
-        at = j < end ? j + 1 : end;
+    uint64_t steps[kWindowSchemes] = {0};
+    const size_t widths[3] = {32, 256, 1024};
+    for (int wi = 0; wi < 3; ++wi) {
+        s = s0;
+        for (size_t at = 0; at < n; ++steps[wi]) {
+            const size_t end = std::min(at + widths[wi], n);
+            size_t j = end;
+            for (size_t k = at; k < end && j == end; ++k)
+                if (bound(s, E[k])) j = k;
+            if (j < end) update(s, E[j]);
+            at = j < end ? j + 1 : end;
+        }
     }
-    uint64_t windows = 0;
-    s = s0;
-    for (size_t at = 0; at < n; ++windows) {
+    uint64_t busy = 0;
+    // one speculative window from `at` (32 candidates at most); returns the next position
+    auto window = [&](St &st, size_t at, std::vector<size_t> &acc, bool count) {
         const int w = (int)(std::min(at + 32, n) - at);
         bool tent[32];
         St chain[33];
-        chain[0] = s;
+        chain[0] = st;
         int nt = 0;
         for (int l = 0; l < w; ++l) {
-            tent[l] = bound(s, E[at + l]);
+            tent[l] = bound(st, E[at + l]);
             if (tent[l]) {
                 chain[nt + 1] = chain[nt];
                 update(chain[nt + 1], E[at + l]);
@@ -969,34 +977,52 @@ void Finder::count_windows(const Clump &c, const std::vector<uint32_t> &near) {
         for (int l = 0; l < w && m < 0; ++l) {
             if (bound(chain[below], E[at + l]) != tent[l]) m = l;
             else if (tent[l]) {
-                spec.push_back(at + l);
+                acc.push_back(at + l);
                 ++below;
                 ++kept;
             }
         }
-        s = chain[below];
+        st = chain[below];
+        size_t next = at + (size_t)w;
         if (m >= 0) {
-            ++window_stats.mismatch_windows;
+            if (count) ++window_stats.mismatch_windows;
             if (!tent[m]) {  // the exact state binds it
-                update(s, E[at + m]);
-                spec.push_back(at + m);
+                update(st, E[at + m]);
+                acc.push_back(at + m);
                 ++kept;
             }
-            at += (size_t)m + 1;
-        } else {
-            at += (size_t)w;
+            next = at + (size_t)m + 1;
         }
-        ++window_stats.accepted_per_window[kept];
+        if (count) {
+            ++window_stats.accepted_per_window[kept];
+            if (kept) ++busy;
+        }
+        return next;
+    };
+    std::vector<size_t> spec3, spec4;
+    s = s0;
+    for (size_t at = 0; at < n; ++steps[3]) at = window(s, at, spec3, true);
+    s = s0;
+    for (size_t at = 0; at < n; ++steps[4]) {
+        const size_t end = std::min(at + 256, n);
+        size_t f = end;
+        for (size_t k = at; k < end && f == end; ++k)
+            if (bound(s, E[k])) f = k;
+        at = f < end ? window(s, f, spec4, false) : end;
     }
     WindowStats &ws = window_stats;
     ws.calls++;
     ws.candidates += n;
     ws.accepted += seq.size();
-    ws.first_bound_steps += first_bound;
-    ws.first_bound_max = std::max(ws.first_bound_max, first_bound);
-    ws.speculative_steps += windows;
-    ws.speculative_max = std::max(ws.speculative_max, windows);
-    if (spec != seq) ws.disagreements++;
+    auto &pc = ws.per_clump[c.peak_index];
+    pc.accepted += seq.size();
+    pc.busy_windows += busy;
+    for (int k = 0; k < kWindowSchemes; ++k) {
+        ws.steps[k] += steps[k];
+        ws.longest_call[k] = std::max(ws.longest_call[k], steps[k]);
+        pc.steps[k] += steps[k];
+    }
+    if (spec3 != seq || spec4 != seq) ws.disagreements++;
 }
 
 void Finder::search_bound_in_hill(Clump &c) {  // src/tree.hpp:4678-4711

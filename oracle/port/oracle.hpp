@@ -197,15 +197,21 @@ struct Stats {
     uint64_t zero_key_quirk = 0;
 };
 
-// Acceptance-window statistics of the Hill rebinding (a study mode, PLAN_ORACLE_WINDOW_STATS=1):
-// each call's candidate sequence replayed with 32-candidate windows, the way the device's
-// default acceptance loop and its speculative windows step through it.
+// Acceptance-step statistics of the Hill rebinding (a study mode, PLAN_ORACLE_WINDOW_STATS=1):
+// each call's candidate sequence replayed with the reference's test and update under several
+// ways a device can step through it (kWindowSchemes; see Finder::count_windows).
+constexpr int kWindowSchemes = 5;
 struct WindowStats {
     uint64_t calls = 0, candidates = 0, accepted = 0;
-    uint64_t first_bound_steps = 0, first_bound_max = 0;      // test 32, take the first bound one, restart after it
-    uint64_t speculative_steps = 0, speculative_max = 0;      // decide 32 against one state, verify, keep the agreeing prefix
-    uint64_t mismatch_windows = 0, disagreements = 0;         // windows cut short; calls whose result differed (must be 0)
+    uint64_t steps[kWindowSchemes] = {0};          // over every call
+    uint64_t longest_call[kWindowSchemes] = {0};   // the most steps one call takes
+    uint64_t mismatch_windows = 0, disagreements = 0;  // windows cut short; calls whose result differed (must be 0)
     uint64_t accepted_per_window[33] = {0};
+    struct PerClump {
+        uint64_t accepted = 0, steps[kWindowSchemes] = {0};
+        uint64_t busy_windows = 0;  // speculative windows (scheme 3) that accept at least one candidate
+    };
+    std::map<uint32_t, PerClump> per_clump;  // by peak, over all the clump's calls
 };
 
 struct Finder {

@@ -2,6 +2,7 @@
 // line (src/global.cpp:247-289) over the CPU restatement. Test infrastructure only.
 #include "oracle.hpp"
 
+#include <algorithm>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -163,12 +164,38 @@ int main(int argc, char **argv) {
         std::printf("%s\n", summary.c_str());
         if (f.window_stats_on) {
             const WindowStats &w = f.window_stats;
-            std::fprintf(stderr,
-                         "[oracle] Hill rebinding: %llu calls, %llu candidates, %llu accepted; first-bound steps %llu (longest call %llu); "
-                         "speculative windows %llu (longest call %llu), %llu cut short, %llu calls disagreeing\n[oracle] accepted per window:",
+            static const char *names[kWindowSchemes] = {"first bound, 32 wide", "first bound, 256 wide", "first bound, 1024 wide",
+                                                         "speculative windows", "256-wide scan + speculative windows"};
+            std::fprintf(stderr, "[oracle] Hill rebinding: %llu calls, %llu candidates, %llu accepted; %llu windows cut short, %llu calls disagreeing\n",
                          (unsigned long long)w.calls, (unsigned long long)w.candidates, (unsigned long long)w.accepted,
-                         (unsigned long long)w.first_bound_steps, (unsigned long long)w.first_bound_max, (unsigned long long)w.speculative_steps,
-                         (unsigned long long)w.speculative_max, (unsigned long long)w.mismatch_windows, (unsigned long long)w.disagreements);
+                         (unsigned long long)w.mismatch_windows, (unsigned long long)w.disagreements);
+            for (int k = 0; k < kWindowSchemes; ++k) {
+                uint64_t most = 0, most_acc = 0;
+                for (const auto &kv : w.per_clump)
+                    if (kv.second.steps[k] > most) {
+                        most = kv.second.steps[k];
+                        most_acc = kv.second.accepted;
+                    }
+                std::fprintf(stderr, "[oracle]   %-36s steps %llu, longest call %llu, most for one clump %llu (it accepts %llu)\n", names[k],
+                             (unsigned long long)w.steps[k], (unsigned long long)w.longest_call[k], (unsigned long long)most,
+                             (unsigned long long)most_acc);
+            }
+            // a cost model of the longest chain, one clump's calls in a row: a step that
+            // accepts costs A cycles in the default loop (3,200 measured); a step or window
+            // that accepts nothing costs E; a speculative window that accepts costs W plus C
+            // per acceptance for its chain of updates (E, W, C are estimates: the FP32 test
+            // and ballot, the test, reciprocals and verification, two dependent FMAs and
+            // their operands)
+            const double A = 3200, E = 400, W = 1500, Cc = 256;
+            double worst_default = 0, worst_spec = 0;
+            for (const auto &kv : w.per_clump) {
+                const auto &pc = kv.second;
+                worst_default = std::max(worst_default, A * pc.accepted + E * (pc.steps[0] - pc.accepted));
+                worst_spec = std::max(worst_spec, W * pc.busy_windows + Cc * pc.accepted + E * (pc.steps[3] - pc.busy_windows));
+            }
+            std::fprintf(stderr, "[oracle] cost model, longest clump chain: default loop %.3g cycles, speculative windows %.3g cycles\n",
+                         worst_default, worst_spec);
+            std::fprintf(stderr, "[oracle] accepted per speculative window:");
             for (uint64_t v : w.accepted_per_window) std::fprintf(stderr, " %llu", (unsigned long long)v);
             std::fprintf(stderr, "\n");
         }

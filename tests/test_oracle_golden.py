@@ -156,13 +156,15 @@ def test_speculative_windows_replay_the_sequential_loop(name, case_dir, oracle_m
                        check=True)
     assert g["summary"] in r.stdout
     assert (out / "res_planetesimals.txt").read_bytes() == (GOLDEN / name / "planetesimals.txt").read_bytes()
-    st = re.search(r"(\d+) calls, (\d+) candidates, (\d+) accepted; first-bound steps (\d+) \(longest call \d+\); "
-                   r"speculative windows (\d+) \(longest call \d+\), (\d+) cut short, (\d+) calls disagreeing", r.stderr)
+    st = re.search(r"(\d+) calls, (\d+) candidates, (\d+) accepted; (\d+) windows cut short, (\d+) calls disagreeing", r.stderr)
     assert st, r.stderr
-    calls, cands, acc, first_bound, windows, cut, disagree = map(int, st.groups())
+    calls, cands, acc, cut, disagree = map(int, st.groups())
     assert calls > 0 and acc > 0
     assert disagree == 0
-    assert windows <= first_bound
+    steps = {m.group(1).strip(): int(m.group(2)) for m in re.finditer(r"\]   (.+?) steps (\d+),", r.stderr)}
+    assert len(steps) == 5, r.stderr
+    assert steps["speculative windows"] <= steps["first bound, 32 wide"]
+    assert steps["first bound, 1024 wide"] <= steps["first bound, 256 wide"] <= steps["first bound, 32 wide"]
 
 
 @pytest.mark.parametrize("keep", [(0, 0), (20, 0)], ids=["empty", "20_particles"])
