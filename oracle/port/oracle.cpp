@@ -1026,10 +1026,23 @@ void Finder::count_windows(const Clump &c, const std::vector<uint32_t> &near) {
 }
 
 void Finder::search_bound_in_hill(Clump &c) {  // src/tree.hpp:4678-4711
-    const Params &p = *par;
     std::vector<uint32_t> near;
     tree.ball(c.center_of_mass, c.Hill_radius, near);
-    if (window_stats_on) count_windows(c, near);
+    if (window_stats_on) {
+        count_windows(c, near);
+        auto &pc = window_stats.per_clump[c.peak_index];
+        pc.calls++;
+        const size_t members_before = c.indices.size();
+        search_bound_in_hill_loop(c, near);
+        if (c.indices.size() > members_before) pc.grown_members += c.indices.size();
+        return;
+    }
+    search_bound_in_hill_loop(c, near);
+}
+
+// The acceptance loop over the ball's points and the final SortParticles (src/tree.hpp:4686-4710).
+void Finder::search_bound_in_hill_loop(Clump &c, const std::vector<uint32_t> &near) {
+    const Params &p = *par;
     for (uint32_t idx : near) {
         TreePoint &t = tree.pts[idx];
         if (t.in_clump_flag || t.new_density < density_threshold) continue;

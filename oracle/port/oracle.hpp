@@ -210,6 +210,7 @@ struct WindowStats {
     struct PerClump {
         uint64_t accepted = 0, steps[kWindowSchemes] = {0};
         uint64_t busy_windows = 0;  // speculative windows (scheme 3) that accept at least one candidate
+        uint64_t calls = 0, grown_members = 0;  // calls; members summed over the calls that grew (re-sorted after each)
     };
     std::map<uint32_t, PerClump> per_clump;  // by peak, over all the clump's calls
 };
@@ -249,6 +250,7 @@ struct Finder {
     void merge(Clump &pred, Clump &prey) const;
     void remove_unbound(Clump &c) const;
     void search_bound_in_hill(Clump &c);
+    void search_bound_in_hill_loop(Clump &c, const std::vector<uint32_t> &near);
     bool window_stats_on = false;
     WindowStats window_stats;
     void count_windows(const Clump &c, const std::vector<uint32_t> &near);

@@ -195,6 +195,17 @@ int main(int argc, char **argv) {
             }
             std::fprintf(stderr, "[oracle] cost model, longest clump chain: default loop %.3g cycles, speculative windows %.3g cycles\n",
                          worst_default, worst_spec);
+            uint64_t most_calls = 0, most_grown = 0, grown_of_most_calls = 0;
+            for (const auto &kv : w.per_clump) {
+                if (kv.second.calls > most_calls) {
+                    most_calls = kv.second.calls;
+                    grown_of_most_calls = kv.second.grown_members;
+                }
+                most_grown = std::max(most_grown, kv.second.grown_members);
+            }
+            std::fprintf(stderr,
+                         "[oracle] calls of one clump, at most %llu (members re-sorted over them: %llu); most members re-sorted for one clump %llu\n",
+                         (unsigned long long)most_calls, (unsigned long long)grown_of_most_calls, (unsigned long long)most_grown);
             std::fprintf(stderr, "[oracle] accepted per speculative window:");
             for (uint64_t v : w.accepted_per_window) std::fprintf(stderr, " %llu", (unsigned long long)v);
             std::fprintf(stderr, "\n");
