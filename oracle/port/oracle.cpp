@@ -1017,6 +1017,7 @@ void Finder::count_windows(const Clump &c, const std::vector<uint32_t> &near) {
     auto &pc = ws.per_clump[c.peak_index];
     pc.accepted += seq.size();
     pc.busy_windows += busy;
+    pc.call.push_back({(uint64_t)seq.size(), steps[0], steps[3], busy});
     for (int k = 0; k < kWindowSchemes; ++k) {
         ws.steps[k] += steps[k];
         ws.longest_call[k] = std::max(ws.longest_call[k], steps[k]);

@@ -12,6 +12,7 @@
 // reference project.
 #pragma once
 
+#include <array>
 #include <cstdint>
 #include <map>
 #include <string>
@@ -211,6 +212,8 @@ struct WindowStats {
         uint64_t accepted = 0, steps[kWindowSchemes] = {0};
         uint64_t busy_windows = 0;  // speculative windows (scheme 3) that accept at least one candidate
         uint64_t calls = 0, grown_members = 0;  // calls; members summed over the calls that grew (re-sorted after each)
+        // per call: accepted, steps of schemes 0 and 3, busy windows (for the round model)
+        std::vector<std::array<uint64_t, 4>> call;
     };
     std::map<uint32_t, PerClump> per_clump;  // by peak, over all the clump's calls
 };

@@ -195,6 +195,23 @@ int main(int argc, char **argv) {
             }
             std::fprintf(stderr, "[oracle] cost model, longest clump chain: default loop %.3g cycles, speculative windows %.3g cycles\n",
                          worst_default, worst_spec);
+            // the round model: every clump makes its k-th call in round k, and a round lasts as
+            // long as its slowest call
+            double round_default = 0, round_spec = 0;
+            for (size_t k = 0;; ++k) {
+                double md = -1, ms = -1;
+                for (const auto &kv : w.per_clump) {
+                    if (k >= kv.second.call.size()) continue;
+                    const auto &q = kv.second.call[k];
+                    md = std::max(md, A * q[0] + E * (q[1] - q[0]));
+                    ms = std::max(ms, W * q[3] + Cc * q[0] + E * (q[2] - q[3]));
+                }
+                if (md < 0) break;
+                round_default += md;
+                round_spec += ms;
+            }
+            std::fprintf(stderr, "[oracle] cost model, rounds (one call per clump per round): default loop %.3g cycles, speculative windows %.3g cycles\n",
+                         round_default, round_spec);
             uint64_t most_calls = 0, most_grown = 0, grown_of_most_calls = 0;
             for (const auto &kv : w.per_clump) {
                 if (kv.second.calls > most_calls) {
