@@ -112,6 +112,7 @@ def lib() -> C.CDLL:
             "plan_catalogue_write_parlists": (i32, [vp, vp, i32, u32]),
             "plan_ctx_release": (i32, [vp]),
             "plan_group_energies": (i32, [vp, vp, vp, vp, vp, u32, C.POINTER(Params), vp, vp, C.POINTER(C.c_uint64)]),
+            "plan_density_vs_scale": (i32, [vp, C.POINTER(Params), C.c_double, dp, dp, i32, C.POINTER(C.c_int32)]),
             "plan_server_create": (i32, [i32, i32, u64, C.POINTER(vp)]),
             "plan_server_destroy": (None, [vp]),
             "plan_submit": (i32, [vp, C.POINTER(LisView), C.POINTER(Params), i32, C.POINTER(C.c_uint64)]),
@@ -145,7 +146,7 @@ EXPORTED = [
     "plan_lis_time", "plan_lis_get_view", "plan_ctx_create", "plan_ctx_destroy", "plan_last_error", "plan_footprint_bytes",
     "plan_build_tree", "plan_find_planetesimals", "plan_find_clumps", "plan_catalogue_free", "plan_catalogue_count",
     "plan_catalogue_get", "plan_catalogue_summary", "plan_catalogue_write_peaks", "plan_catalogue_write_parlists",
-    "plan_catalogue_basic_results", "plan_ctx_release", "plan_group_energies", "plan_server_create", "plan_server_destroy", "plan_submit", "plan_poll",
+    "plan_catalogue_basic_results", "plan_ctx_release", "plan_group_energies", "plan_density_vs_scale", "plan_server_create", "plan_server_destroy", "plan_submit", "plan_poll",
     "plan_server_error", "plan_server_stats",
     "plan_stage_count", "plan_stage_copy", "plan_knn", "plan_morton_order", "plan_morton_order_noalloc", "plan_stage_times", "plan_kernel_launches", "plan_counters",
     "plan_synth_default_spec", "plan_synth_records", "plan_synth_write_lis", "plan_synth_four_pi_G_for_mean",
@@ -350,6 +351,18 @@ class Finder:
         if rc:
             raise PlanError(rc, self.error())
         return ek, ep, int(z.value)
+
+    def density_vs_scale(self, p: Params, time: float):
+        """--Density_Vs_Scale on the tree of the last build_tree, which must have run with
+        p.density_vs_scale = 1: (radii, densities), one per length scale."""
+        radii = np.zeros(32)
+        rho = np.zeros(32)
+        nlev = C.c_int32()
+        rc = lib().plan_density_vs_scale(self._h, C.byref(p), float(time), radii.ctypes.data_as(C.POINTER(C.c_double)),
+                                         rho.ctypes.data_as(C.POINTER(C.c_double)), 32, C.byref(nlev))
+        if rc:
+            raise PlanError(rc, self.error())
+        return radii[:nlev.value].copy(), rho[:nlev.value].copy()
 
     def write_parlists(self, cat: "Catalogue", file_number: int = 0, sampling: int = 1) -> None:
         """The --Save_Clumps member lists of cat (ParList.<NNNN>/ in the working directory),

@@ -107,6 +107,29 @@ def test_cli_density_vs_scale(name, case, extra, built, tmp_path):
     assert cases.parlist_digests(out) == meta["parlist"]
 
 
+def test_density_vs_scale_through_the_binding(built, tmp_path):
+    """plan_density_vs_scale called directly (Finder.density_vs_scale) on a tree built for it:
+    the radii and densities equal the oracle's, which equal the reference's, bit for bit."""
+    import oracle
+
+    name, case, _ = cases.DVS[2]  # the sheared one, at t = 0.37
+    m = cases.materialise(case, tmp_path / "in")
+    p = built.params(m["param"])
+    p.density_vs_scale = 1
+    snap = built.Snapshot(m["lis"])
+    f = built.Finder(0)
+    try:
+        f.build_tree(snap, p)
+        radii, rho = f.density_vs_scale(p, snap.view.time)
+    finally:
+        f.close()
+        snap.close()
+    o = oracle.Oracle(m["lis"], m["param"], threads=1, density_vs_scale=True)
+    r_o, v_o = o.density_vs_scale()
+    assert radii.tobytes() == r_o.tobytes()
+    assert rho.tobytes() == v_o.tobytes()
+
+
 def test_cli_two_snapshots_density_vs_scale(built, tmp_path):
     """The drop-in binary over two snapshots with --Density_Vs_Scale alone writes the
     reference's files (one RMPL header, lines and basic results interleaved)."""

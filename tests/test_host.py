@@ -219,6 +219,36 @@ def test_cli_parameter_file_errors_before_device(built, tmp_path):
     assert r.returncode == 3
 
 
+def test_entry_points_refuse_null_handles(built):
+    """Every entry point that takes a context, a server or a catalogue checks it before any
+    device work: a null one is an argument error (status 2), as are zero workers."""
+    import ctypes as C
+
+    L = built.lib()
+    p = built.params()
+    v = built.LisView()
+    out, n, u64, d = C.c_void_p(), C.c_int32(), C.c_uint64(), C.c_double()
+    got = {
+        "plan_build_tree": L.plan_build_tree(None, C.byref(v), C.byref(p), 1, None),
+        "plan_find_planetesimals": L.plan_find_planetesimals(None, C.byref(p), None, C.byref(out)),
+        "plan_find_clumps": L.plan_find_clumps(None, C.byref(v), C.byref(p), 1, None, C.byref(out)),
+        "plan_density_vs_scale": L.plan_density_vs_scale(None, C.byref(p), 0.0, None, None, 0, C.byref(n)),
+        "plan_group_energies": L.plan_group_energies(None, None, None, None, None, 0, C.byref(p), None, None, None),
+        "plan_catalogue_write_parlists": L.plan_catalogue_write_parlists(None, None, 0, 1),
+        "plan_ctx_release": L.plan_ctx_release(None),
+        "plan_submit": L.plan_submit(None, C.byref(v), C.byref(p), 1, C.byref(u64)),
+        "plan_poll": L.plan_poll(None, 1, 0, C.byref(out), C.byref(d)),
+        "plan_server_stats": L.plan_server_stats(None, None, None),
+        "plan_knn": L.plan_knn(None, None, 0, 32, 0.0, None, None),
+        "plan_morton_order": L.plan_morton_order(None, None, 0, None),
+        "plan_morton_order_noalloc": L.plan_morton_order_noalloc(None, None, 0, None),
+        "plan_stage_times": L.plan_stage_times(None, None, 0),
+        "plan_counters": L.plan_counters(None, None, 0),
+        "plan_server_create (0 workers)": L.plan_server_create(0, 0, 0, C.byref(out)),
+    }
+    assert got == {k: 2 for k in got}
+
+
 def test_no_device_no_fallback(built):
     """Without a CUDA device every device entry point fails with status 5: the context, the
     serving loop, and so every computation behind them. There is no CPU path to fall back on."""
