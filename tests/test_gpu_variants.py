@@ -11,6 +11,7 @@ from __future__ import annotations
 import json
 import os
 import subprocess
+import sys
 
 import pytest
 
@@ -107,27 +108,37 @@ def test_cli_density_vs_scale(name, case, extra, built, tmp_path):
     assert cases.parlist_digests(out) == meta["parlist"]
 
 
+_DVS_CHILD = """
+import json, sys
+sys.path.insert(0, sys.argv[1])
+import plan_gb300 as pg
+lis, param = json.loads(sys.argv[2]), sys.argv[3]
+p = pg.params(param)
+p.density_vs_scale = 1
+snap = pg.Snapshot(lis)
+f = pg.Finder(0)
+f.build_tree(snap, p)
+radii, rho = f.density_vs_scale(p, snap.view.time)
+print(json.dumps([radii.tobytes().hex(), rho.tobytes().hex()]))
+"""
+
+
 def test_density_vs_scale_through_the_binding(built, tmp_path):
-    """plan_density_vs_scale called directly (Finder.density_vs_scale) on a tree built for it:
-    the radii and densities equal the oracle's, which equal the reference's, bit for bit."""
+    """plan_density_vs_scale called directly (Finder.density_vs_scale, in a child process) on
+    a tree built for it: the radii and densities equal the oracle's, which equal the
+    reference's, bit for bit."""
     import oracle
 
     name, case, _ = cases.DVS[2]  # the sheared one, at t = 0.37
     m = cases.materialise(case, tmp_path / "in")
-    p = built.params(m["param"])
-    p.density_vs_scale = 1
-    snap = built.Snapshot(m["lis"])
-    f = built.Finder(0)
-    try:
-        f.build_tree(snap, p)
-        radii, rho = f.density_vs_scale(p, snap.view.time)
-    finally:
-        f.close()
-        snap.close()
+    r = subprocess.run([sys.executable, "-c", _DVS_CHILD, str(ROOT), json.dumps(m["lis"]), m["param"]], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stderr
+    radii_hex, rho_hex = json.loads(r.stdout.strip().splitlines()[-1])
     o = oracle.Oracle(m["lis"], m["param"], threads=1, density_vs_scale=True)
     r_o, v_o = o.density_vs_scale()
-    assert radii.tobytes() == r_o.tobytes()
-    assert rho.tobytes() == v_o.tobytes()
+    assert radii_hex == r_o.tobytes().hex()
+    assert rho_hex == v_o.tobytes().hex()
 
 
 def test_cli_two_snapshots_density_vs_scale(built, tmp_path):
