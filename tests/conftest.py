@@ -2,6 +2,8 @@
 from __future__ import annotations
 
 import json
+import os
+import subprocess
 import sys
 from pathlib import Path
 
@@ -58,3 +60,16 @@ def case_dir(tmp_path_factory, built):
 
 def golden(name: str) -> dict:
     return json.loads((GOLDEN / name / "meta.json").read_text())
+
+
+def run_isolated(request) -> bool:
+    """Run the calling test again in a child pytest process, so that a device fault in it
+    ends only that process and not the tests collected after it. Returns True in the parent,
+    after asserting that the child passed (the child runs with --runxfail, so an expected
+    failure fails it); returns False in the child, which then runs the test body."""
+    if os.environ.get("PLAN_TEST_CHILD") == "1":
+        return False
+    r = subprocess.run([sys.executable, "-m", "pytest", "-q", "-x", "--runxfail", "-p", "no:cacheprovider", request.node.nodeid],
+                       cwd=ROOT, env=dict(os.environ, PLAN_TEST_CHILD="1"), capture_output=True, text=True, timeout=1800)
+    assert r.returncode == 0, (r.stdout[-4000:] + r.stderr[-2000:])
+    return True

@@ -10,6 +10,7 @@ from __future__ import annotations
 import pytest
 
 import cases
+from conftest import run_isolated
 from test_gpu_parity import check_cli_drop_in, check_stages_and_catalogue
 
 # Written after this build's last GPU run: until a GPU run has passed them, a failure is
@@ -20,16 +21,15 @@ pytestmark = [pytest.mark.gpu, pytest.mark.xfail(reason="not yet run on a GPU", 
 SPLINE = [c.name for c in cases.SPLINE]
 
 
-@pytest.fixture(scope="module")
-def finder(built):
-    f = built.Finder(0)
-    yield f
-    f.close()
-
-
 @pytest.mark.parametrize("name", SPLINE)
-def test_spline_stages_and_catalogue(name, built, finder, case_dir, tmp_path):
-    check_stages_and_catalogue(name, built, finder, case_dir, tmp_path)
+def test_spline_stages_and_catalogue(name, request, built, case_dir, tmp_path):
+    if run_isolated(request):
+        return
+    f = built.Finder(0)
+    try:
+        check_stages_and_catalogue(name, built, f, case_dir, tmp_path)
+    finally:
+        f.close()
 
 
 @pytest.mark.parametrize("name", SPLINE[:1])

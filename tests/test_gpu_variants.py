@@ -11,12 +11,11 @@ from __future__ import annotations
 import json
 import os
 import subprocess
-import sys
 
 import pytest
 
 import cases
-from conftest import GOLDEN, ROOT, golden
+from conftest import GOLDEN, ROOT, golden, run_isolated
 
 # Written after this build's last GPU run: until a GPU run has passed them, a failure is
 # reported as XFAIL (and does not stop the suite before the tests that have passed); a pass
@@ -43,9 +42,11 @@ def test_cli_variants(name, case, extra, built, tmp_path):
 
 
 @pytest.mark.parametrize("name,sampling", [("w1_20k", 1), ("w1_20k_sinks", 1), ("w1_20k", 3)])
-def test_device_member_lists(name, sampling, built, case_dir, tmp_path, monkeypatch):
+def test_device_member_lists(name, sampling, request, built, case_dir, tmp_path, monkeypatch):
     """Member lists formatted on the device equal the host-formatted ones byte for byte (and
     so the reference's): same files, same lines, every sub-sampling."""
+    if run_isolated(request):
+        return
     m = case_dir(name)
     p = built.params(m["param"])
     snap = built.Snapshot(m["lis"])
@@ -108,37 +109,29 @@ def test_cli_density_vs_scale(name, case, extra, built, tmp_path):
     assert cases.parlist_digests(out) == meta["parlist"]
 
 
-_DVS_CHILD = """
-import json, sys
-sys.path.insert(0, sys.argv[1])
-import plan_gb300 as pg
-lis, param = json.loads(sys.argv[2]), sys.argv[3]
-p = pg.params(param)
-p.density_vs_scale = 1
-snap = pg.Snapshot(lis)
-f = pg.Finder(0)
-f.build_tree(snap, p)
-radii, rho = f.density_vs_scale(p, snap.view.time)
-print(json.dumps([radii.tobytes().hex(), rho.tobytes().hex()]))
-"""
-
-
-def test_density_vs_scale_through_the_binding(built, tmp_path):
-    """plan_density_vs_scale called directly (Finder.density_vs_scale, in a child process) on
-    a tree built for it: the radii and densities equal the oracle's, which equal the
-    reference's, bit for bit."""
+def test_density_vs_scale_through_the_binding(request, built, tmp_path):
+    """plan_density_vs_scale called directly (Finder.density_vs_scale) on a tree built for it:
+    the radii and densities equal the oracle's, which equal the reference's, bit for bit."""
+    if run_isolated(request):
+        return
     import oracle
 
     name, case, _ = cases.DVS[2]  # the sheared one, at t = 0.37
     m = cases.materialise(case, tmp_path / "in")
-    r = subprocess.run([sys.executable, "-c", _DVS_CHILD, str(ROOT), json.dumps(m["lis"]), m["param"]], capture_output=True, text=True,
-                       timeout=300)
-    assert r.returncode == 0, r.stderr
-    radii_hex, rho_hex = json.loads(r.stdout.strip().splitlines()[-1])
+    p = built.params(m["param"])
+    p.density_vs_scale = 1
+    snap = built.Snapshot(m["lis"])
+    f = built.Finder(0)
+    try:
+        f.build_tree(snap, p)
+        radii, rho = f.density_vs_scale(p, snap.view.time)
+    finally:
+        f.close()
+        snap.close()
     o = oracle.Oracle(m["lis"], m["param"], threads=1, density_vs_scale=True)
     r_o, v_o = o.density_vs_scale()
-    assert radii_hex == r_o.tobytes().hex()
-    assert rho_hex == v_o.tobytes().hex()
+    assert radii.tobytes() == r_o.tobytes()
+    assert rho.tobytes() == v_o.tobytes()
 
 
 def test_cli_two_snapshots_density_vs_scale(built, tmp_path):

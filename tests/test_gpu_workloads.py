@@ -17,7 +17,7 @@ import time
 
 import pytest
 
-from conftest import GOLDEN, golden
+from conftest import GOLDEN, golden, run_isolated
 
 # Written after this build's last GPU run: until a GPU run has passed them, a failure is
 # reported as XFAIL (and does not stop the suite before the tests that have passed); a pass
@@ -49,7 +49,9 @@ def _poll_until(srv, rid, seconds):
 
 
 @pytest.mark.parametrize("workers,budget_of_largest", [(3, 0.0), (2, 1.2)])
-def test_mixed_requests_match_alone(workers, budget_of_largest, built, case_dir, tmp_path):
+def test_mixed_requests_match_alone(workers, budget_of_largest, request, built, case_dir, tmp_path):
+    if run_isolated(request):
+        return
     pg = built
     cases_m = {n: case_dir(n) for n in MIX}
     snaps = {n: pg.Snapshot(m["lis"]) for n, m in cases_m.items()}
@@ -91,7 +93,9 @@ def test_mixed_requests_match_alone(workers, budget_of_largest, built, case_dir,
             s.close()
 
 
-def test_oversized_request_is_refused(built, case_dir):
+def test_oversized_request_is_refused(request, built, case_dir):
+    if run_isolated(request):
+        return
     pg = built
     m = case_dir("w1_20k")
     snap = pg.Snapshot(m["lis"])
@@ -105,7 +109,9 @@ def test_oversized_request_is_refused(built, case_dir):
         snap.close()
 
 
-def test_group_energies_against_fp64(built):
+def test_group_energies_against_fp64(request, built):
+    if run_isolated(request):
+        return
     import numpy as np
 
     from test_energy_host import fp64_potential_sum, plummer_group
