@@ -197,8 +197,8 @@ int plan_submit(plan_server *srv, const plan_lis_view *snap, const plan_params *
  * blocks until done), or the request's error status with its message in
  * plan_server_error. A request is returned once. */
 int plan_poll(plan_server *srv, uint64_t request, int wait, plan_catalogue **out, double *latency_ms);
-/* Message of the last failed request returned by plan_poll on this server; valid until the
- * next failed plan_poll or plan_submit on it. */
+/* Message of the last failed request returned by plan_poll on this server (or of a refused
+ * plan_submit), copied for the calling thread: valid until that thread calls this again. */
 const char *plan_server_error(const plan_server *srv);
 /* Largest sum of worker holds seen against the budget, and how many holds were given back. */
 int plan_server_stats(const plan_server *srv, uint64_t *peak_held_bytes, uint64_t *releases);

@@ -133,9 +133,12 @@ int plan_poll(plan_server *srv, uint64_t request, int wait, plan_catalogue **out
 }
 
 const char *plan_server_error(const plan_server *srv) {
+    // a copy per calling thread: another thread may replace the server's message meanwhile
+    static thread_local std::string copy;
     if (!srv) return "no server";
     std::lock_guard<std::mutex> lk(srv->mu);
-    return srv->error.c_str();
+    copy = srv->error;
+    return copy.c_str();
 }
 
 int plan_server_stats(const plan_server *srv, uint64_t *peak_held_bytes, uint64_t *releases) {
