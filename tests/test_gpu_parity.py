@@ -11,7 +11,6 @@ from __future__ import annotations
 
 import os
 import subprocess
-from pathlib import Path
 
 import numpy as np
 import pytest
