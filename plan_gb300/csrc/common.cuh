@@ -19,7 +19,7 @@ enum Status : int {
     kErrParameter = 4,    // bad parameter (exit(4))
     kErrDevice = 5,       // CUDA error
     kErrOutOfMemory = 6,  // device allocation failed / admission refused
-    kErrUnsupported = 7,  // input outside what this build handles (reported, never faked)
+    kErrUnsupported = 7,  // input outside what this library handles (reported, never faked)
     kErrDeviceLimit = 8,  // a bounded device loop ran out (error flag set by a kernel)
 };
 

@@ -5,7 +5,7 @@
 // (WriteBasicResults), peaks_at_<time>.txt and, with --Save_Clumps, ParList.<NNNN>/.
 // -x/-y/-z user boxes restrict the particles read, as in the reference. --Density_Vs_Scale
 // writes <out>_RMPL.txt and finds clumps on that run's tree, as the reference does. The grid
-// analyses (--Basic_Analyses, --Temp_Calculation) are not part of this build and are rejected
+// analyses (--Basic_Analyses, --Temp_Calculation) are not part of this program and are rejected
 // with exit code 2.
 #include <cstdio>
 #include <cstdlib>
@@ -164,7 +164,7 @@ int main(int argc, char **argv) {
         return 2;
     }
     if (f_basic || f_tmp) {
-        std::cerr << "Error: only --Find_Clumps and --Density_Vs_Scale are available in this build (the grid analyses are not part of it)."
+        std::cerr << "Error: only --Find_Clumps and --Density_Vs_Scale are available in this program (the grid analyses are not part of it)."
                   << std::endl;
         return 2;
     }
