@@ -81,3 +81,12 @@ def test_boundness_groups():
     assert len(sizes) == 20 and sizes.min() >= 32 and sizes.max() <= 2000
     assert pos.shape == (int(off[-1]), 3) and vel.shape == pos.shape and mass.shape == (int(off[-1]),)
     assert pos.dtype == np.float32 and mass.dtype == np.float32
+
+
+def test_cpu_sample_runs_warmups_then_times(built):
+    """The CPU legs generate the sample snapshot once, run the warm-up passes untimed and
+    return one time per timed pass (read to catalogue through the oracle)."""
+    import bench
+
+    r = bench.cpu_sample(20000, 3, 2, reps=2, warmup=1)
+    assert r["n"] == 20000 and len(r["seconds"]) == 2 and min(r["seconds"]) > 0
