@@ -417,8 +417,15 @@ def run_serve(args) -> None:
     th.start()
     th.join()
     served_lat, same = [], True
+    deadline = time.monotonic() + 300.0 + 20.0 * plain_s  # a request that never finishes ends the run
     for i in range(len(reqs)):
-        cat, lat = srv.poll(ids[i], wait=True)
+        got = srv.poll(ids[i])
+        while got is None and time.monotonic() < deadline:
+            time.sleep(0.005)
+            got = srv.poll(ids[i])
+        if got is None:
+            raise SystemExit(f"bench.py --serve: request {i} not done by the deadline")
+        cat, lat = got
         served_lat.append(lat)
         same = same and cat.summary() == plain_sum[i]
         cat.close()
