@@ -69,7 +69,9 @@ def run_isolated(request) -> bool:
     failure fails it); returns False in the child, which then runs the test body."""
     if os.environ.get("PLAN_TEST_CHILD") == "1":
         return False
-    r = subprocess.run([sys.executable, "-m", "pytest", "-q", "-x", "--runxfail", "-p", "no:cacheprovider", request.node.nodeid],
+    path = getattr(request.node, "path", None) or request.node.fspath  # absolute, whatever the parent's rootdir
+    node = f"{path}::{request.node.name}"
+    r = subprocess.run([sys.executable, "-m", "pytest", "-q", "-x", "--runxfail", "-p", "no:cacheprovider", node],
                        cwd=ROOT, env=dict(os.environ, PLAN_TEST_CHILD="1"), capture_output=True, text=True, timeout=1800)
     assert r.returncode == 0, (r.stdout[-4000:] + r.stderr[-2000:])
     return True
