@@ -97,14 +97,9 @@ int density_vs_scale(Context &c, const plan_params &p, double time, std::vector<
     std::vector<double> xs, ys, zs;
     const int src = dvs_setup(dp, time, key_to_double(ext[0]), key_to_double(ext[1]), g, xs, ys, zs);
     if (src) {
-        c.last_error = src == -1 ? "density vs scale: the grid gives more radii than supported"
-                                 : "density vs scale: the points or the box need more than 2^24 cell centres along an axis";
-        return kErrUnsupported;
-    }
-    // one thread per query: at most 2^31 - 1 blocks of 128 (each axis is below 2^24, so the
-    // product is checked in double before it is formed in 64 bits)
-    if ((double)g.nx * g.ny * g.nz * g.nvar > 2147483647.0 * 128.0) {
-        c.last_error = "density vs scale: the grid has more queries than one launch can take";
+        c.last_error = src == -1   ? "density vs scale: the grid gives more radii than supported"
+                       : src == -2 ? "density vs scale: the points or the box need more than 2^24 cell centres along an axis"
+                                   : "density vs scale: the grid has more queries than one launch can take";
         return kErrUnsupported;
     }
     std::vector<uint32_t> maxc(g.nlev, 0);

@@ -48,7 +48,8 @@ struct DvsParams {
 // accumulated x += cell as its loops do). zlo, zhi: extreme z of the tree points. 0; -1 when
 // the grid gives more radii than kDvsMaxLevels; -2 when an axis would need more than 2^24
 // centres (coordinates far outside any box the parameters describe, where the reference's
-// loops would run for ever).
+// loops would run for ever); -3 when the queries (one device thread each) would need more
+// than 2^31 - 1 blocks of 128.
 inline int dvs_setup(const DvsParams &p, double time, double zlo, double zhi, DvsGeom &g, std::vector<double> &xs, std::vector<double> &ys,
                      std::vector<double> &zs) {
     g = DvsGeom{};
@@ -89,6 +90,8 @@ inline int dvs_setup(const DvsParams &p, double time, double zlo, double zhi, Dv
     g.nx = (uint32_t)xs.size();
     g.ny = (uint32_t)ys.size();
     g.nz = (uint32_t)zs.size();
+    // each axis is below 2^24, so the product is checked in double before it is formed in 64 bits
+    if ((double)g.nx * g.ny * g.nz * g.nvar > 2147483647.0 * 128.0) return -3;
     return 0;
 }
 

@@ -36,6 +36,18 @@ struct HostTree {
     void point(uint32_t q, double &x, double &y, double &z) const { x = p3[3 * q]; y = p3[3 * q + 1]; z = p3[3 * q + 2]; }
 };
 
+extern "C" int dvs_setup_status(const double *q19, double time, double zlo, double zhi) {
+    plan::DvsParams p;
+    for (int d = 0; d < 3; ++d) {
+        p.box_length[d] = q19[d]; p.box_min[d] = q19[3 + d]; p.box_max[d] = q19[6 + d]; p.box_center[d] = q19[9 + d];
+        p.cell_length[d] = q19[14 + d];
+    }
+    p.box_half_width0 = q19[12]; p.max_half_width = q19[13]; p.shear_speed = q19[17]; p.mass_per_particle0 = q19[18];
+    plan::DvsGeom g;
+    std::vector<double> xs, ys, zs;
+    return plan::dvs_setup(p, time, zlo, zhi, g, xs, ys, zs);
+}
+
 extern "C" int dvs_host(const double *f4, const uint32_t *u7, const double *p3, uint32_t np, const double *q19, double time, double *radii,
                         double *rho, int cap) {
     plan::DvsParams p;
@@ -116,3 +128,25 @@ def test_device_dvs_arithmetic_matches_oracle(name, shim, oracle_mod, tmp_path):
     rmpl = (GOLDEN / name / "res_RMPL.txt").read_text().splitlines()
     assert rmpl[1] == "%15.6e" % time + "".join("%15.6e" % x for x in v_h[:n])
     assert meta["files"]
+
+
+def test_dvs_setup_refuses_grids_it_cannot_launch(shim, oracle_mod, tmp_path):
+    """The grid set-up's limits, on a golden's parameters with ever finer cells: the golden's
+    own grid is accepted; 2^21 centres per axis give more queries than one launch takes (-3);
+    more than 2^24 centres along an axis are refused before they are made (-2)."""
+    import ctypes as C
+
+    shim.dvs_setup_status.restype = C.c_int
+    shim.dvs_setup_status.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double]
+    _, case, _ = cases.DVS[0]
+    m = cases.materialise(case, tmp_path / "in")
+    o = oracle_mod.Oracle(m["lis"], m["param"], threads=1, pow_mode=0, density_vs_scale=True)
+    q19 = np.ascontiguousarray(o.density_vs_scale_params(), dtype=np.float64)
+    zlo, zhi = -0.01, 0.01
+    assert shim.dvs_setup_status(q19.ctypes.data, 0.0, zlo, zhi) == 0
+    fine = q19.copy()
+    fine[14:17] = q19[0:3] / 2.0**21
+    assert shim.dvs_setup_status(fine.ctypes.data, 0.0, zlo, zhi) == -3
+    finer = q19.copy()
+    finer[14:17] = q19[0:3] / 2.0**25
+    assert shim.dvs_setup_status(finer.ctypes.data, 0.0, zlo, zhi) == -2
