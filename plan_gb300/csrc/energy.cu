@@ -130,12 +130,8 @@ int group_energies(Context &c, const float *pos3, const float *vel3, const float
                    double shear_y, double *e_kin, double *e_pot, uint64_t *zero_pairs, cudaStream_t s) {
     if (ngroups == 0) return kOk;
     const uint64_t n = offsets[ngroups];
-    std::vector<uint64_t> item_off(ngroups + 1, 0);
-    for (uint32_t g = 0; g < ngroups; ++g) {
-        if (offsets[g + 1] < offsets[g]) return kErrArgument;
-        const uint64_t T = (offsets[g + 1] - offsets[g] + kPairTile - 1) / kPairTile;
-        item_off[g + 1] = item_off[g] + T * (T + 1) / 2;
-    }
+    std::vector<uint64_t> item_off;
+    if (pair_items(offsets, ngroups, item_off)) return kErrArgument;
     const uint64_t nitems = item_off[ngroups];
     std::vector<float4> hpm(n), hv(n);
     for (uint64_t i = 0; i < n; ++i) {

@@ -4,6 +4,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <vector>
 
 #ifdef __CUDACC__
 #define PLAN_EN_HD __host__ __device__
@@ -18,6 +19,20 @@ constexpr int kPairTile = 128;
 // Tile (ti, tj), tj >= ti, of the upper triangle of a T x T tiling, with tiles numbered row
 // by row: row ti starts at ti T - ti (ti - 1) / 2.
 PLAN_EN_HD inline uint64_t tri_row_start(uint64_t T, uint64_t k) { return k * T - k * (k - 1) / 2; }
+
+// The tile queue over all groups: item_off[g] is the first queue item of group g, whose
+// n_g = offsets[g+1] - offsets[g] particles make T (T + 1) / 2 tiles of the upper triangle
+// (T = ceil(n_g / kPairTile)); item_off[ngroups] is the number of items. -1 when the offsets
+// decrease.
+inline int pair_items(const uint64_t *offsets, uint32_t ngroups, std::vector<uint64_t> &item_off) {
+    item_off.assign((size_t)ngroups + 1, 0);
+    for (uint32_t g = 0; g < ngroups; ++g) {
+        if (offsets[g + 1] < offsets[g]) return -1;
+        const uint64_t T = (offsets[g + 1] - offsets[g] + kPairTile - 1) / kPairTile;
+        item_off[g + 1] = item_off[g] + T * (T + 1) / 2;
+    }
+    return 0;
+}
 
 PLAN_EN_HD inline void tile_of(uint64_t local, uint64_t T, uint64_t &ti, uint64_t &tj) {
     const double a = 2.0 * (double)T + 1.0;

@@ -25,6 +25,13 @@ SHIM = r"""
 
 using namespace plan;
 
+extern "C" int pair_items_host(const uint64_t *offsets, uint32_t ngroups, uint64_t *out) {
+    std::vector<uint64_t> v;
+    const int rc = pair_items(offsets, ngroups, v);
+    for (size_t i = 0; i < v.size(); ++i) out[i] = v[i];
+    return rc;
+}
+
 extern "C" int tiles_cover(uint64_t T) {
     std::vector<uint8_t> seen(T * T, 0);
     const uint64_t n = T * (T + 1) / 2;
@@ -143,3 +150,16 @@ def test_coincident_pairs_left_out(shim):
         ok = d > 0
         tot += float((m[i] * m[i + 1:][ok] / d[ok]).sum())
     assert abs(got - tot) <= 1e-6 * tot and keep.all()
+
+
+def test_pair_items_over_groups(shim):
+    """The tile queue over all groups: each group's T (T + 1) / 2 upper-triangle tiles of 128,
+    empty groups none, and decreasing offsets refused."""
+    shim.pair_items_host.restype = C.c_int
+    shim.pair_items_host.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p]
+    off = np.array([0, 0, 1, 129, 300, 300 + 128 * 5], dtype=np.uint64)
+    out = np.zeros(len(off), dtype=np.uint64)
+    assert shim.pair_items_host(off.ctypes.data, len(off) - 1, out.ctypes.data) == 0
+    assert out.tolist() == [0, 0, 1, 2, 5, 20]  # n = 0, 1, 128, 171, 640: T = 0, 1, 1, 2, 5
+    bad = np.array([0, 10, 5], dtype=np.uint64)
+    assert shim.pair_items_host(bad.ctypes.data, 2, out.ctypes.data) == -1
