@@ -94,14 +94,16 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
 
 
 def build_oracle(reference_src: str | None = None) -> None:
-    """Build the CPU restatement (always) and the reference oracle (when its sources exist)."""
+    """Build the CPU restatement (always) and the reference oracle when the reference's
+    src/ directory is given (argument, else the PLAN_REF_SRC environment variable) and holds
+    its sources."""
     _run(["make", "-C", str(ROOT / "oracle"), "port"])
-    ref = Path(reference_src or "/root/reference/src")
-    if (ref / "tree.hpp").exists():
-        _run(["make", "-C", str(ROOT / "oracle"), "ref", f"REF_SRC={ref}"])
+    src = reference_src or os.environ.get("PLAN_REF_SRC")
+    if src and (Path(src) / "tree.hpp").exists():
+        _run(["make", "-C", str(ROOT / "oracle"), "ref", f"REF_SRC={Path(src).resolve()}"])
 
 
 if __name__ == "__main__":
     build(verbose=True)
-    build_oracle()
+    build_oracle(sys.argv[1] if len(sys.argv) > 1 else None)
     sys.exit(0)

@@ -930,6 +930,8 @@ __device__ void defer_add(uint32_t *dset, uint8_t *dover, uint32_t *dmax, uint32
     dover[slot] = 1;
 }
 
+#include "rebind_loop.cuh"
+
 // One SearchBoundParticlesWithinHillRadius call for every listed clump (one block each).
 // seq_mode = 1: the reference's shared in-clump flags, one clump at a time.
 // seq_mode = 0: clumps run concurrently. owner[q] holds the key rank of the clump holding
@@ -1905,7 +1907,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
     ct.sub_head = A.get<uint32_t>(C + 1); ct.sub_tail = A.get<uint32_t>(C + 1);
     Pool &P = st.P;
     const uint32_t m0 = hg.n_members;
-    P.cap = (uint32_t)std::min<uint64_t>(0xfffffff0ull, 3ull * m0 + Tu / 4 + 4096);
+    P.cap = (uint32_t)std::min<uint64_t>(0xfffffff0ull, 6ull * m0 + Tu + 4096);
     P.idx = A.get<uint32_t>(P.cap);
     P.dist = A.get<double>(P.cap);
     st.alt_idx = A.get<uint32_t>(P.cap);
@@ -2292,6 +2294,114 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
         const bool rcp = rcp_env && *rcp_env == '1';
         auto rebind_kernel = speculate ? k_rebind_round<1> : rcp ? k_rebind_round<2> : k_rebind_round<0>;
         uint64_t rounds = 0, passes = 0, reruns = 0;
+        // Each clump's calls run on the device (k_rebind_loop), one launch per pass; the
+        // round-by-round host loop (one launch and one host round trip per call) stays
+        // available with PLAN_REBIND_ROUNDS=1 for comparison.
+        const char *rounds_env = std::getenv("PLAN_REBIND_ROUNDS");
+        const bool use_rounds = rounds_env && *rounds_env == '1';
+        uint8_t *d_fin = A.get<uint8_t>(nb), *d_susp = A.get<uint8_t>(nb), *d_needsort = A.get<uint8_t>(nb), *d_distsq = A.get<uint8_t>(nb);
+        uint32_t *d_head = A.get<uint32_t>(4), *d_blkoff = A.get<uint32_t>(nb + 1);
+        unsigned long long *d_rstats = trace.on ? A.get<unsigned long long>(8 * nb) : nullptr;
+        double4_32a *tm0 = use_rounds ? nullptr : A.get<double4_32a>(Tu), *tm1 = use_rounds ? nullptr : A.get<double4_32a>(Tu);
+        if (A.failed) return kErrOutOfMemory;
+        int rb_grid = 1;
+        if (!use_rounds) {
+            k_member_terms<<<grid_for(Tu, 256), 256, 0, s>>>(Tu, tr.pos, tr.vel, tm0, tm1);
+            c.launches++;
+            PLAN_CUDA(cudaMemsetAsync(d_needsort, 0, nb, s));
+            PLAN_CUDA(cudaMemsetAsync(d_distsq, 0, nb, s));
+            if (d_rstats) PLAN_CUDA(cudaMemsetAsync(d_rstats, 0, 8 * nb * 8, s));
+            int dev = 0, nsm = 0, per = 0;
+            PLAN_CUDA(cudaGetDevice(&dev));
+            PLAN_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+            PLAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rebind_loop, kRB, 0));
+            rb_grid = std::max(1, nsm * std::max(1, per));
+        }
+        uint64_t loop_launches = 0, suspensions = 0;
+        // One pass of the device loop over `list` (key-rank order). Clumps that found the
+        // member pool full stop with a consistent state; the pool is compacted and they
+        // continue in another launch.
+        auto run_loop = [&](const std::vector<uint32_t> &list, const std::vector<std::vector<uint32_t>> *blk) -> int {
+            std::vector<uint32_t> todo = list;
+            int stuck = 0;
+            for (int attempt = 0; !todo.empty(); ++attempt) {
+                if (attempt > 4096 || stuck > 3) return kErrOutOfMemory;
+                std::vector<uint8_t> fin(nb, 1);
+                for (uint32_t sl : todo) fin[sl] = 0;
+                PLAN_CUDA(cudaMemcpyAsync(d_fin, fin.data(), nb, cudaMemcpyHostToDevice, s));
+                PLAN_CUDA(cudaMemsetAsync(d_head, 0, 4, s));
+                int r = st.up_list(todo, st.d_list);
+                if (r) return r;
+                Arena &S = c.scratch;
+                const size_t mark = S.used;
+                uint32_t *d_blk = nullptr;
+                const bool with_blk = blk != nullptr && attempt == 0;
+                std::vector<uint32_t> off, lst;  // kept alive until the launch has read them
+                if (with_blk) {
+                    off.assign(todo.size() + 1, 0);
+                    for (size_t i = 0; i < todo.size(); ++i) {
+                        for (uint32_t b : (*blk)[todo[i]]) lst.push_back(b);
+                        off[i + 1] = (uint32_t)lst.size();
+                    }
+                    d_blk = S.get<uint32_t>(lst.size() + 1);
+                    if (S.failed || !d_blk) { S.used = mark; return kErrOutOfMemory; }
+                    PLAN_CUDA(cudaMemcpyAsync(d_blkoff, off.data(), off.size() * 4, cudaMemcpyHostToDevice, s));
+                    if (!lst.empty()) PLAN_CUDA(cudaMemcpyAsync(d_blk, lst.data(), lst.size() * 4, cudaMemcpyHostToDevice, s));
+                }
+                RbArgs ra;
+                ra.list = st.d_list;
+                ra.n = (uint32_t)todo.size();
+                ra.head = d_head;
+                ra.blk_off = with_blk ? d_blkoff : nullptr;
+                ra.blk = d_blk;
+                ra.finished = d_fin;
+                ra.suspended = d_susp;
+                ra.needsort = d_needsort;
+                ra.distsq = d_distsq;
+                ra.stats = d_rstats;
+                ra.ct = ct;
+                ra.P = P;
+                ra.t = kt;
+                ra.ft = ftr;
+                ra.vel = tr.vel;
+                ra.tm0 = tm0;
+                ra.tm1 = tm1;
+                ra.E = E;
+                ra.epos = epos;
+                ra.owner = owner;
+                ra.rank_of = rank_of;
+                ra.tent = tent;
+                ra.dmax = dmax;
+                ra.dset = dset;
+                ra.dover = dover;
+                ra.com0 = bc;
+                ra.reach = reach;
+                ra.cp = st.cp;
+                ra.err = c.d_err;
+                const unsigned grid = (unsigned)std::min<size_t>(todo.size(), (size_t)rb_grid);
+                double t_a = wall_ms();
+                k_rebind_loop<<<grid, kRB, 0, s>>>(ra);
+                c.launches++;
+                ++loop_launches;
+                PLAN_CUDA(cudaGetLastError());
+                std::vector<uint8_t> sus;
+                r = st.down(sus, d_susp, nb);
+                S.used = mark;
+                if (r) return r;
+                c.stage_ms[16] += wall_ms() - t_a;
+                std::vector<uint32_t> next;
+                for (uint32_t sl : todo)
+                    if (sus[sl]) next.push_back(sl);
+                if (!next.empty()) {
+                    suspensions += next.size();
+                    stuck = next.size() == todo.size() ? stuck + 1 : 0;
+                    r = st.maybe_compact(true);
+                    if (r) return r;
+                }
+                todo.swap(next);
+            }
+            return kOk;
+        };
         // Rounds until no clump grows. Clumps in `waiting` start once every clump listed as
         // their blocker has finished (reruns in key order where their balls may meet).
         std::vector<uint8_t> finished(C, 0);
@@ -2440,7 +2550,33 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                 active.swap(first);
             }
             const std::vector<uint32_t> ran = pass > 0 ? active_all : live;
-            rc = run_rounds(active, 0, waiting, (pass > 0 && schedule_reruns) ? blockers : no_blockers);
+            if (use_rounds) {
+                rc = run_rounds(active, 0, waiting, (pass > 0 && schedule_reruns) ? blockers : no_blockers);
+            } else {
+                // reruns wait on the device for the lower-ranked reruns they met in the last
+                // pass (PLAN_RERUN_SCHEDULE=0: all start at once)
+                rc = run_loop(active_all, (pass > 0 && !(sched_env && *sched_env == '0')) ? &blockers : nullptr);
+                if (!rc && trace.on) {
+                    std::vector<unsigned long long> rs;
+                    rc = st.down(rs, d_rstats, 8 * nb);
+                    if (!rc) {
+                        size_t worst = 0;
+                        unsigned long long wt = 0, calls = 0, acc = 0;
+                        for (uint32_t sl : active_all) {
+                            const unsigned long long *q = &rs[8 * (size_t)sl];
+                            calls += q[0];
+                            acc += q[2];
+                            if (q[3] + q[4] + q[5] > wt) { wt = q[3] + q[4] + q[5]; worst = sl; }
+                        }
+                        const unsigned long long *w = &rs[8 * worst];
+                        std::fprintf(stderr,
+                                     "[plan]   loop pass %u: %zu clumps, %llu calls, %llu accepted (cumulative); worst clump: calls %llu cand %llu acc %llu "
+                                     "kcycles search %llu accept %llu sort %llu (sums+dist %llu) sorts %llu\n",
+                                     (unsigned)pass, active_all.size(), calls, acc, w[0], w[1], w[2], w[3] / 1000, w[4] / 1000, w[5] / 1000,
+                                     w[6] / 1000, w[7]);
+                    }
+                }
+            }
             if (rc) return rc;
             if (!live.empty()) {  // every clump: a running one may have taken a particle from any later one
                 rc = st.up_list(live, st.d_list2);
@@ -2554,6 +2690,8 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
             reruns += rerun.size();
             PLAN_CUDA(cudaMemcpyAsync(rerun_rank, rr.data(), nlive, cudaMemcpyHostToDevice, s));
             k_rebind_tentative<<<grid_for(Tu, 256), 256, 0, s>>>(Tu, owner, tent, rerun_rank);
+            rc = st.maybe_compact();  // room for the restored segments
+            if (rc) return rc;
             rc = st.up_list(rerun, st.d_list2);
             if (rc) return rc;
             k_rebind_restore<<<(unsigned)rerun.size(), 256, 0, s>>>(st.d_list2, (uint32_t)rerun.size(), ct, P, bM, bh, bri, bro, br10, br2,
@@ -2563,9 +2701,10 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
             active = rerun;
         }
         // final ownership = the reference's in-clump marks of rebinding
-        c.stage_ms[14] = (double)rounds;
+        c.stage_ms[14] = (double)(use_rounds ? rounds : loop_launches);
         c.counters[14] = reruns;
         c.counters[12] = passes;
+        c.counters[23] = suspensions;
     }
     PLAN_CUDA(cudaStreamSynchronize(s));
     double tw3 = wall_ms();

@@ -19,6 +19,8 @@
 
 #include <cstdint>
 
+#include "exact64.cuh"
+
 namespace plan {
 
 // s + x[0] + x[1] + ... + x[n-1], left to right with rounding after every add. Called by all
@@ -73,6 +75,52 @@ __device__ inline double warp_ordered_sum(const double *x, uint32_t n, double s)
         }
         const long long na = __shfl_sync(full, nn, a - 1);
         s = (double)na * u;  // |na| <= 2^53: exact
+        k += (uint32_t)a;
+    }
+    return s;
+}
+
+// The same sum with the grid rounding of the terms and the result done in integer
+// arithmetic (grid_term, grid_value): no FP64 instruction except for the ordinary adds
+// that start a run or step over a tie, a binade change or an out-of-range running sum.
+__device__ inline double warp_ordered_sum_int(const double *x, uint32_t n, double s) {
+    const int lane = threadIdx.x & 31;
+    const unsigned full = 0xffffffffu;
+    uint32_t k = 0;
+    while (k < n) {
+        const long long bits = __double_as_longlong(s);
+        const uint32_t ex = (uint32_t)((bits >> 52) & 0x7ff);
+        if (ex <= 60 || ex >= 2000) {  // zero, tiny or huge: no grid, one ordinary add
+            s = s + x[k];
+            ++k;
+            continue;
+        }
+        const long long mag = (bits & 0xfffffffffffffLL) | (1LL << 52);
+        const long long n0 = bits < 0 ? -mag : mag;  // s / u
+        const uint32_t j = k + lane;
+        long long nj = 0;
+        const bool ok = j < n && grid_term(x[j], ex, nj);
+        long long p = ok ? nj : 0;
+        for (int d = 1; d < 32; d <<= 1) {
+            const long long t = __shfl_up_sync(full, p, d);
+            if (lane >= d) p += t;
+        }
+        const long long nn = n0 + p;
+        const long long an = nn < 0 ? -nn : nn;
+        const bool inside = ok && ((nn < 0) == (n0 < 0)) && an > (1LL << 52) && an <= (1LL << 53);
+        const unsigned valid = __ballot_sync(full, j < n);
+        const unsigned good = __ballot_sync(full, inside);
+        const unsigned top = __ballot_sync(full, inside && an == (1LL << 53));
+        const unsigned bad = valid & ~good;
+        int a = bad ? __ffs(bad) - 1 : __popc(valid);
+        if (top) a = min(a, __ffs(top));  // stop after the first lane that reached 2^(e+1)
+        if (a == 0) {
+            s = s + x[k];
+            ++k;
+            continue;
+        }
+        const long long na = __shfl_sync(full, nn, a - 1);
+        s = grid_value(na, ex);
         k += (uint32_t)a;
     }
     return s;

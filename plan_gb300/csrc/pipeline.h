@@ -122,7 +122,7 @@ int launch_densest(Context &c, const plan_params &p, uint32_t k, double threshol
 
 // Device bytes kept per tree point over a snapshot (tree, nodes, HOP and clump buffers),
 // and the scratch bytes per input particle; used for sizing and for admission.
-constexpr uint64_t kArenaBytesPerTreePoint = 360;
+constexpr uint64_t kArenaBytesPerTreePoint = 512;
 constexpr uint64_t kScratchBytesPerParticle = 160;
 
 inline unsigned grid_for(size_t n, int threads) {

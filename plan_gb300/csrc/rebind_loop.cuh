@@ -1,0 +1,742 @@
+// Hill-sphere rebinding with every clump's calls on the device (src/tree.hpp:4196-4208).
+//
+// The reference runs, clump by clump in key order,
+//     do { SearchBoundParticlesWithinHillRadius; CalculateHillRadius; } while (it grew)
+// where a call that accepts anything ends with SortParticles (src/tree.hpp:4678-4711,
+// 4446-4512, 4715-4717). k_rebind_loop runs that whole loop for a clump inside one block:
+// a persistent grid takes clumps from a queue in key-rank order, so a host round trip is
+// needed only per pass, not per call. Clumps of one launch run concurrently under the
+// ordered-claim rule of the round kernel (owner / tent / defer records); a clump may first
+// wait for lower-ranked clumps it met in the previous pass (its blockers). Those were taken
+// from the queue before it by running blocks, so every wait ends; each wait is bounded all
+// the same and reports kDevErrLoopLimit if it runs out.
+//
+// Inside a call:
+//  * ball search: the breadth-first frontier of the round kernel, then one block-wide pass
+//    over the eligible points of every frontier entry (a contained node keeps all of them,
+//    a boundary node keeps those in the ball), compacted in point order;
+//  * acceptance: warp 0 tests 32 staged candidates at a time in FP32 (FP64 when too close
+//    to call) and takes the first bound one. The state update is the reference's FP64
+//    formula; its division is a reciprocal product with Markstein's correction, the
+//    reciprocals of the next masses taken 32 at a time off the dependent chain while all
+//    accepted particles have the same mass;
+//  * SortParticles: the seven member sums in member order (warp_ordered_sum_int over
+//    per-point products m, m x, ..., m vz formed once per snapshot), the centre of mass and
+//    the Hill radius, squared distances, and a stable sort by squared distance (in shared
+//    memory up to kSmallSort members, else a block radix sort on the top 32 bits followed
+//    by an exact fix-up of equal prefixes). Squared distances order members as distances
+//    do, except that two squared distances may round to one distance: neighbours within a
+//    few ulps are compared through their square roots, and a tie goes to the library-order
+//    replay exactly as in the round kernels. The square roots of the last sort are taken
+//    when the clump's loop ends.
+#pragma once
+
+constexpr int kRB = 256;                      // threads of a rebinding block
+constexpr uint32_t kWaitLimit = 1u << 25;     // bounded waits on blockers (about 30 s)
+constexpr uint32_t kCallLimit = 1u << 20;     // calls of one clump in one launch
+
+struct RbArgs {
+    const uint32_t *list;  // clumps of this launch, in key-rank order
+    uint32_t n;
+    uint32_t *head;        // next queue position
+    const uint32_t *blk_off, *blk;  // blockers of list[i]: blk[blk_off[i], blk_off[i+1]) (slots); null: none
+    uint8_t *finished;     // per slot: its calls are done in this launch (or it is not in it)
+    uint8_t *suspended;    // per slot: stopped because the member pool is full (state consistent)
+    uint8_t *needsort;     // per slot: the last call grew the clump but its SortParticles is pending
+    uint8_t *distsq;       // per slot: the segment's distances are still squared
+    unsigned long long *stats;  // per slot, 8 counters (may be null)
+    CT ct;
+    Pool P;
+    KTree t;
+    FTree ft;
+    const double4_32a *vel;
+    const double4_32a *tm0, *tm1;  // per point: (m, m x, m y, m z), (m vx, m vy, m vz, 0)
+    const uint32_t *E, *epos;
+    uint32_t *owner;
+    const uint32_t *rank_of, *tent;
+    uint32_t *dmax, *dset;
+    uint8_t *dover;
+    const double4_32a *com0;
+    unsigned long long *reach;
+    CP cp;
+    unsigned *err;
+};
+
+// per-point products for the member sums (src/tree.hpp:4436-4440: mass, pos * mass,
+// vel * mass, each component rounded once)
+__global__ void k_member_terms(uint32_t Tu, const double4_32a *pos, const double4_32a *vel, double4_32a *tm0, double4_32a *tm1) {
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= Tu) return;
+    const double4_32a p = pos[q], v = vel[q];
+    tm0[q] = make_double4_32a(p.w, p.x * p.w, p.y * p.w, p.z * p.w);
+    tm1[q] = make_double4_32a(v.x * p.w, v.y * p.w, v.z * p.w, 0.0);
+}
+
+__device__ __forceinline__ void split_any(double x, float &h, float &l) {
+    if (!split_hilo_bits(x, h, l)) split_f(x, h, l);
+}
+
+// block-wide compaction offset of this thread's flag; returns the block total
+__device__ __forceinline__ uint32_t rb_block_rank(bool keep, uint32_t &rank, uint32_t *warp_tot) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const unsigned b = __ballot_sync(0xffffffffu, keep);
+    if (lane == 0) warp_tot[wid] = __popc(b);
+    __syncthreads();
+    uint32_t before = 0, total = 0;
+    for (int w = 0; w < kRB / 32; ++w) {
+        const uint32_t c = warp_tot[w];
+        if (w < wid) before += c;
+        total += c;
+    }
+    rank = before + __popc(b & ((1u << lane) - 1u));
+    __syncthreads();
+    return total;
+}
+
+struct RbShared {
+    unsigned char *buf;  // kFront * 14 bytes, reused by every phase
+    uint32_t *warp_tot;
+    uint32_t *u;         // scalars
+    double *st;          // M, com x y z, vcom x y z, hill
+    double *tabM, *tabY;
+    float *tabF;
+};
+
+// ------------------------------------------------------------------ one SearchBound call
+// Returns the number of accepted particles, or kNone when the member pool is full (nothing
+// changed).
+__device__ uint32_t rb_call(const RbArgs &a, uint32_t slot, uint32_t myrank, RbShared &sh, unsigned long long *stat) {
+    const int tid = threadIdx.x, lane = tid & 31;
+    uint32_t *front = reinterpret_cast<uint32_t *>(sh.buf), *front2 = front + kFront, *fcnt = front2 + kFront;
+    uint8_t *fcls = reinterpret_cast<uint8_t *>(fcnt + kFront), *fcls2 = fcls + kFront;
+    uint32_t &s_nf = sh.u[0], &s_expand = sh.u[1], &s_noff = sh.u[2], &s_nel = sh.u[3], &s_nacc = sh.u[4], &s_m0 = sh.u[5],
+             &s_o = sh.u[6], &s_S = sh.u[7];
+    const long long t0 = clock64();
+    if (tid == 0) {
+        const double4_32a c = a.ct.com[slot], v = a.ct.vcom[slot];
+        sh.st[0] = a.ct.M[slot];
+        sh.st[1] = c.x; sh.st[2] = c.y; sh.st[3] = c.z;
+        sh.st[4] = v.x; sh.st[5] = v.y; sh.st[6] = v.z;
+        sh.st[7] = a.ct.hill[slot];
+        s_m0 = a.ct.mn[slot];
+        s_o = a.ct.moff[slot];
+        front[0] = 0;
+        fcls[0] = 0;
+        s_nf = 1;
+        s_nel = 0;
+        s_nacc = 0;
+        const double4_32a c0 = a.com0[slot];  // how far this clump's balls reach from its centre before rebinding
+        const double dx = c.x - c0.x, dy = c.y - c0.y, dz = c.z - c0.z;
+        const double d = sqrt(dx * dx + dy * dy + dz * dz) + sh.st[7];
+        if (d >= 0) atomicMax(&a.reach[slot], (unsigned long long)__double_as_longlong(d));
+    }
+    __syncthreads();
+    const BallQ ball = make_ball(sh.st[1], sh.st[2], sh.st[3], sh.st[7]);
+    const KTree &t = a.t;
+    // 1) breadth-first frontier (classes 1..4; 0 = not yet classified)
+    for (int level = 0; level < 40; ++level) {
+        const uint32_t nf = s_nf;
+        if (tid == 0) s_expand = 0;
+        __syncthreads();
+        for (uint32_t i = tid; i < nf; i += kRB) {
+            const uint32_t node = front[i];
+            int cls = fcls[i];
+            if (cls == 0) {
+                if (node >= t.nodes) {
+                    atomicOr(a.err, (unsigned)kDevErrBadNode);
+                    cls = 3;
+                } else {
+                    uint32_t eb, ee;
+                    cls = ball_class(t, a.ft, a.epos, node, ball, eb, ee);
+                }
+                fcls[i] = (uint8_t)cls;
+            }
+            fcnt[i] = cls == 4 ? t.nnd[node] : (cls == 3 ? 0u : 1u);
+            if (cls == 4) s_expand = 1;
+        }
+        __syncthreads();
+        if (!s_expand) break;
+        const uint32_t total = block_scan_excl(fcnt, nf, sh.warp_tot);
+        if (total > (uint32_t)kFront) break;
+        for (uint32_t i = tid; i < nf; i += kRB) {
+            const int cls = fcls[i];
+            const uint32_t o = fcnt[i];
+            if (cls == 1 || cls == 2) {
+                front2[o] = front[i];
+                fcls2[o] = (uint8_t)cls;
+            } else if (cls == 4) {
+                const uint32_t c0 = t.nfd[front[i]], nc = t.nnd[front[i]];
+                for (uint32_t c = 0; c < nc; ++c) {
+                    front2[o + c] = c0 + c;
+                    fcls2[o + c] = 0;
+                }
+            }
+        }
+        __syncthreads();
+        for (uint32_t i = tid; i < total; i += kRB) {
+            front[i] = front2[i];
+            fcls[i] = fcls2[i];
+        }
+        if (tid == 0) s_nf = total;
+        __syncthreads();
+    }
+    const uint32_t nf = s_nf;
+    // 2) each entry's slice of eligible points: its start (front2) and length (fcnt), scanned
+    for (uint32_t i = tid; i < nf; i += kRB) {
+        uint32_t eb = 0, ee = 0;
+        int cls = fcls[i];
+        if (front[i] >= t.nodes) {
+            cls = 3;
+        } else if (cls == 0) {
+            cls = ball_class(t, a.ft, a.epos, front[i], ball, eb, ee);
+        } else {
+            eb = a.epos[t.nbeg[front[i]]];
+            ee = a.epos[t.nend[front[i]]];
+        }
+        fcls[i] = (uint8_t)cls;
+        front2[i] = eb;
+        fcnt[i] = cls == 3 ? 0u : ee - eb;
+    }
+    __syncthreads();
+    const uint32_t S = block_scan_excl(fcnt, nf, sh.warp_tot);
+    // 3) the new segment: the members, then room for every scanned point
+    if (tid == 0) {
+        s_S = S;
+        s_noff = pool_try_alloc(a.P, s_m0 + S);
+    }
+    __syncthreads();
+    if (s_noff == kNone) return kNone;
+    const uint32_t m0 = s_m0, o = s_o, no = s_noff;
+    for (uint32_t k = tid; k < m0; k += kRB) a.P.idx[no + k] = a.P.idx[o + k];
+    uint32_t *elig = a.P.idx + no + m0;
+    for (uint32_t base = 0; base < S; base += kRB) {
+        const uint32_t tt = base + tid;
+        bool keep = false;
+        uint32_t q = 0;
+        if (tt < S) {
+            uint32_t lo = 0, hi = nf;  // the last entry starting at or before tt
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (fcnt[mid] <= tt) lo = mid;
+                else hi = mid;
+            }
+            q = a.E[front2[lo] + (tt - fcnt[lo])];
+            keep = fcls[lo] == 1 || in_ball(t, a.ft, ball, q);
+        }
+        uint32_t r;
+        const uint32_t tot = rb_block_rank(keep, r, sh.warp_tot);
+        if (keep) elig[s_nel + r] = q;
+        __syncthreads();
+        if (tid == 0) s_nel += tot;
+        __syncthreads();
+    }
+    const uint32_t nel = s_nel;
+    const long long t1 = clock64();
+    // 4) the reference's sequential acceptance (src/tree.hpp:4686-4706)
+    double4_32a *tpos = reinterpret_cast<double4_32a *>(sh.buf), *tvel = tpos + kTile;
+    CandF *tf = reinterpret_cast<CandF *>(tvel + kTile);
+    uint32_t *tq = reinterpret_cast<uint32_t *>(tf + kTile);
+    uint8_t *ttaken = reinterpret_cast<uint8_t *>(tq + kTile);
+    const float G32 = (float)a.cp.G, shear32 = (float)a.cp.shear;
+    double M = 0, comp = 0;          // warp 0: the mass and, in lane c < 6, component c of the state
+    float Mf = 0.f, shv[6], slv[6];  // its float forms
+    double tab_m = -1.0;             // the mass the reciprocal table was built for
+    int tab_n = 0, tab_i = 0;
+    uint32_t nacc = 0;
+    if (tid < 32) {
+        M = sh.st[0];
+        comp = lane < 6 ? sh.st[1 + lane] : 0.0;
+        float h = 0.f, l = 0.f;
+        split_any(comp, h, l);
+        for (int c = 0; c < 6; ++c) {
+            shv[c] = __shfl_sync(0xffffffffu, h, c);
+            slv[c] = __shfl_sync(0xffffffffu, l, c);
+        }
+        float mh, ml;
+        split_any(M, mh, ml);
+        Mf = mh;
+    }
+    for (uint32_t base = 0; base < nel; base += kTile) {
+        const uint32_t tend = min(nel, base + (uint32_t)kTile);
+        for (uint32_t i = tid; base + i < tend; i += kRB) {
+            const uint32_t q2 = elig[base + i];
+            const uint32_t ow = __ldcg(&a.owner[q2]), tn = a.tent[q2];
+            const bool taken = (ow != kNone && ow <= myrank) || (tn != kNone && tn < myrank);
+            if (ow != kNone && ow < myrank) defer_add(a.dset, a.dover, a.dmax, slot, ow);
+            else if (tn != kNone && tn < myrank) defer_add(a.dset, a.dover, a.dmax, slot, tn);
+            tq[i] = q2;
+            ttaken[i] = taken ? 1 : 0;
+            const double4_32a pp = t.pos[q2], vv = a.vel[q2];
+            tpos[i] = pp;
+            tvel[i] = vv;
+            const float4 ph = a.ft.phi[q2], pl = a.ft.plo[q2];
+            CandF cf;
+            cf.ph[0] = ph.x; cf.ph[1] = ph.y; cf.ph[2] = ph.z;
+            cf.pl[0] = pl.x; cf.pl[1] = pl.y; cf.pl[2] = pl.z;
+            split_any(vv.x, cf.vh[0], cf.vl[0]);
+            split_any(vv.y, cf.vh[1], cf.vl[1]);
+            split_any(vv.z, cf.vh[2], cf.vl[2]);
+            float wl;
+            split_any(pp.w, cf.w, wl);
+            tf[i] = cf;
+        }
+        __syncthreads();
+        if (tid < 32) {
+            const unsigned full = 0xffffffffu;
+            uint32_t at = base;
+            while (at < tend) {
+                const uint32_t k = at + lane;
+                bool bound = false, unsure = false;
+                if (k < tend && !ttaken[k - base]) {
+                    const int r = bound_hilo(tf[k - base], Mf, shv, slv, G32, shear32);
+                    if (r >= 0) bound = r == 1;
+                    else unsure = true;
+                }
+                if (__any_sync(full, unsure)) {  // the FP64 test needs the whole state in every lane
+                    const double x = __shfl_sync(full, comp, 0), y = __shfl_sync(full, comp, 1), z = __shfl_sync(full, comp, 2);
+                    const double vx = __shfl_sync(full, comp, 3), vy = __shfl_sync(full, comp, 4), vz = __shfl_sync(full, comp, 5);
+                    if (unsure) bound = bound_fp64(tpos[k - base], tvel[k - base], M, x, y, z, vx, vy, vz, a.cp);
+                }
+                const unsigned b = __ballot_sync(full, bound);
+                if (!b) {
+                    at = min(at + 32, tend);
+                    continue;
+                }
+                const int f = __ffs(b) - 1;
+                const uint32_t j = at + f - base;
+                const double m = tpos[j].w;
+                if (!(tab_i < tab_n && m == tab_m)) {
+                    // the next masses M_{l+1} = RN(M_l + m) on the grid of M's binade (exact while
+                    // they stay inside it), and their correctly rounded reciprocals, one per lane
+                    tab_m = m;
+                    tab_i = 0;
+                    tab_n = 0;
+                    const uint64_t mb = dbits(M);
+                    const uint32_t ex = (uint32_t)(mb >> 52) & 0x7ffu;
+                    long long dn = 0;
+                    if (M > 0.0 && m > 0.0 && ex > 60u && ex < 2000u && grid_term(m, ex, dn) && dn > 0) {
+                        const long long n0 = (long long)((mb & 0xfffffffffffffull) | (1ull << 52));
+                        const long long nl = n0 + (long long)(lane + 1) * dn;
+                        const bool ok = nl > (1LL << 52) && nl <= (1LL << 53);
+                        const unsigned okm = __ballot_sync(full, ok);
+                        const unsigned edge = __ballot_sync(full, ok && nl == (1LL << 53));
+                        int cnt = (~okm) ? __ffs(~okm) - 1 : 32;
+                        if (edge) cnt = min(cnt, __ffs(edge));
+                        if (lane < cnt) {
+                            const double Ml = grid_value(nl, ex);
+                            float fh, fl;
+                            split_any(Ml, fh, fl);
+                            sh.tabM[lane] = Ml;
+                            sh.tabY[lane] = __drcp_rn(Ml);
+                            sh.tabF[lane] = fh;
+                        }
+                        tab_n = cnt;
+                        __syncwarp();
+                    }
+                }
+                double Mn, y;
+                float Mnf;
+                if (tab_i < tab_n) {
+                    Mn = sh.tabM[tab_i];
+                    y = sh.tabY[tab_i];
+                    Mnf = sh.tabF[tab_i];
+                    ++tab_i;
+                } else {
+                    Mn = M + m;
+                    y = __drcp_rn(Mn);
+                    float fl;
+                    split_any(Mn, Mnf, fl);
+                    tab_n = 0;
+                }
+                // src/tree.hpp:4696-4701 (the new mass multiplies the old centre): lane c < 6
+                // updates component c as RN(RN(RN(c M') + RN(m q_c)) / M')
+                float h = 0.f, l = 0.f;
+                if (lane < 6) {
+                    const double4_32a p = tpos[j], v = tvel[j];
+                    const double qc = lane == 0 ? p.x : lane == 1 ? p.y : lane == 2 ? p.z : lane == 3 ? v.x : lane == 4 ? v.y : v.z;
+                    const double num = comp * Mn + m * qc;
+                    if (num == 0.0) {
+                        comp = num;  // the quotient keeps the numerator's zero
+                    } else {
+                        const double q0 = num * y;
+                        comp = fma(fma(-q0, Mn, num), y, q0);
+                    }
+                    split_any(comp, h, l);
+                }
+                for (int c = 0; c < 6; ++c) {
+                    shv[c] = __shfl_sync(full, h, c);
+                    slv[c] = __shfl_sync(full, l, c);
+                }
+                M = Mn;
+                Mf = Mnf;
+                if (lane == 0) {
+                    const uint32_t q2 = tq[j];
+                    // the lowest rank keeps the particle; who lost one is found after the pass
+                    atomicMin(&a.owner[q2], myrank);
+                    elig[nacc] = q2;  // accepted ones overwrite candidates already consumed
+                }
+                ++nacc;
+                at += f + 1;
+            }
+        }
+        __syncthreads();
+    }
+    if (tid == 0) s_nacc = nacc;
+    __syncthreads();
+    nacc = s_nacc;
+    const long long t2 = clock64();
+    if (tid == 0) {
+        if (stat) {
+            stat[0] += 1;
+            stat[1] += nel;
+            stat[2] += nacc;
+            stat[3] += (unsigned long long)(t1 - t0);
+            stat[4] += (unsigned long long)(t2 - t1);
+        }
+        if (nacc) {
+            a.ct.moff[slot] = no;
+            a.ct.mn[slot] = m0 + nacc;
+        } else {
+            atomicCAS(a.P.top, no + m0 + S, no);  // give the segment back when nothing was taken after it
+        }
+    }
+    __syncthreads();
+    return nacc;
+}
+
+// ------------------------------------------------------------------ SortParticles
+// Block radix sort (stable, 8-bit digits) of n (key, value) pairs from (ki, vi) into the
+// other buffer pair; digits that are the same for every key are skipped. Returns 0 when
+// the result is in (ki, vi), 1 when in (ko, vo).
+__device__ int rb_radix32(uint32_t *ki, uint32_t *vi, uint32_t *ko, uint32_t *vo, uint32_t n, uint32_t *smem) {
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    uint32_t *hist = smem, *wcnt = smem + 256, *flag = smem + 256 + 256 * (kRB / 32);
+    int where = 0;
+    for (int pass = 0; pass < 4; ++pass) {
+        const int sh = 8 * pass;
+        uint32_t *kin = where ? ko : ki, *vin = where ? vo : vi, *kout = where ? ki : ko, *vout = where ? vi : vo;
+        for (int d = tid; d < 256; d += kRB) hist[d] = 0;
+        for (int d = tid; d < 256 * (kRB / 32); d += kRB) wcnt[d] = 0;
+        if (tid == 0) flag[0] = 0;
+        __syncthreads();
+        for (uint32_t i = tid; i < n; i += kRB) atomicAdd(&hist[(kin[i] >> sh) & 255u], 1u);
+        __syncthreads();
+        for (int d = tid; d < 256; d += kRB)
+            if (hist[d] == n) flag[0] = 1;
+        __syncthreads();
+        if (flag[0]) continue;  // every key has this digit
+        if (tid < 32) {  // exclusive scan of the 256 bins by warp 0, 8 per lane
+            uint32_t v[8], s = 0;
+            for (int q = 0; q < 8; ++q) { v[q] = hist[lane * 8 + q]; s += v[q]; }
+            uint32_t incl = s;
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t u = __shfl_up_sync(0xffffffffu, incl, d);
+                if (lane >= d) incl += u;
+            }
+            uint32_t run = incl - s;
+            for (int q = 0; q < 8; ++q) { hist[lane * 8 + q] = run; run += v[q]; }
+        }
+        __syncthreads();
+        for (uint32_t b = 0; b < n; b += kRB) {
+            const uint32_t i = b + tid;
+            const bool valid = i < n;
+            const uint32_t key = valid ? kin[i] : 0u, val = valid ? vin[i] : 0u;
+            const uint32_t dig = valid ? (key >> sh) & 255u : 256u;
+            const unsigned peers = __match_any_sync(0xffffffffu, dig);
+            const uint32_t rk = __popc(peers & ((1u << lane) - 1u));
+            if (valid && (uint32_t)(__ffs(peers) - 1) == (uint32_t)lane) wcnt[wid * 256 + dig] = __popc(peers);
+            __syncthreads();
+            if (valid) {
+                uint32_t off = hist[dig];
+                for (int w = 0; w < wid; ++w) off += wcnt[w * 256 + dig];
+                kout[off + rk] = key;
+                vout[off + rk] = val;
+            }
+            __syncthreads();
+            for (int d = tid; d < 256; d += kRB) {
+                uint32_t tot = 0;
+                for (int w = 0; w < kRB / 32; ++w) {
+                    tot += wcnt[w * 256 + d];
+                    wcnt[w * 256 + d] = 0;
+                }
+                hist[d] += tot;
+            }
+            __syncthreads();
+        }
+        where ^= 1;
+    }
+    return where;
+}
+
+// any two neighbours of a sorted run of squared distances whose square roots are equal
+__device__ __forceinline__ bool rb_sqrt_tie(double s0, double s1) {
+    if (s0 == s1) return true;
+    const unsigned long long b0 = (unsigned long long)__double_as_longlong(s0), b1 = (unsigned long long)__double_as_longlong(s1);
+    if (b1 - b0 > 64ull) return false;  // more than a few ulps apart: the roots differ
+    return sqrt(s0) == sqrt(s1);
+}
+
+// SortParticles with the Hill radius after it (src/tree.hpp:4446-4512, 4715-4717). Returns
+// false when the pool has no room for a large sort (the clump is then left with needsort).
+__device__ bool rb_sort_particles(const RbArgs &a, uint32_t slot, RbShared &sh, unsigned long long *stat) {
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    uint32_t &s_o = sh.u[8], &s_m = sh.u[9], &s_tie = sh.u[10], &s_r = sh.u[11];
+    const long long t0 = clock64();
+    if (tid == 0) {
+        s_o = a.ct.moff[slot];
+        s_m = a.ct.mn[slot];
+        s_tie = 0;
+    }
+    __syncthreads();
+    const uint32_t o = s_o, m = s_m;
+    uint32_t *idx = a.P.idx + o;
+    double *dist = a.P.dist + o;
+    // 1) the seven sums in member order (CalculateKinematicProperties)
+    double *term = reinterpret_cast<double *>(sh.buf);  // [7][kKinTile]
+    double acc = 0.0;
+    for (uint32_t base = 0; base < m; base += kKinTile) {
+        const uint32_t cnt = min((uint32_t)kKinTile, m - base);
+        for (uint32_t i = tid; i < cnt; i += kRB) {
+            const uint32_t q = idx[base + i];
+            const double4_32a A = a.tm0[q], B = a.tm1[q];
+            term[0 * kKinTile + i] = A.x;
+            term[1 * kKinTile + i] = A.y;
+            term[2 * kKinTile + i] = A.z;
+            term[3 * kKinTile + i] = A.w;
+            term[4 * kKinTile + i] = B.x;
+            term[5 * kKinTile + i] = B.y;
+            term[6 * kKinTile + i] = B.z;
+        }
+        __syncthreads();
+        if (wid < 7) acc = warp_ordered_sum_int(term + wid * kKinTile, cnt, acc);
+        __syncthreads();
+    }
+    if (wid < 7 && lane == 0) sh.tabM[wid] = acc;  // the table is free between calls
+    __syncthreads();
+    if (tid < 32) {
+        const double Ms = sh.tabM[0];
+        double v = 0.0;
+        if (lane >= 1 && lane <= 6) v = sh.tabM[lane] / Ms;
+        if (lane == 7) v = cr_pow_third(Ms * a.cp.G / 3. / a.cp.Omega / a.cp.Omega);  // src/tree.hpp:4715-4717
+        if (lane >= 1 && lane <= 7) sh.st[lane] = v;
+        if (lane == 0) sh.st[0] = Ms;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        a.ct.M[slot] = sh.st[0];
+        a.ct.com[slot] = make_double4_32a(sh.st[1], sh.st[2], sh.st[3], 0);
+        a.ct.vcom[slot] = make_double4_32a(sh.st[4], sh.st[5], sh.st[6], 0);
+        a.ct.hill[slot] = sh.st[7];
+    }
+    // 2) squared distances to the new centre (src/tree.hpp:4448-4450: (pos - com).Norm())
+    const double cx = sh.st[1], cy = sh.st[2], cz = sh.st[3];
+    for (uint32_t k = tid; k < m; k += kRB) {
+        const double4_32a p = a.t.pos[idx[k]];
+        const double dx = p.x - cx, dy = p.y - cy, dz = p.z - cz;
+        double s = dx * dx;
+        s = s + dy * dy;
+        s = s + dz * dz;
+        dist[k] = s;
+    }
+    __syncthreads();
+    const long long t1 = clock64();
+    bool ok = true;
+    if (m <= (uint32_t)kSmallSort) {
+        // 3a) in shared memory: bitonic sort by (squared distance, position)
+        unsigned long long *sk = reinterpret_cast<unsigned long long *>(sh.buf);
+        uint32_t *si = reinterpret_cast<uint32_t *>(sk + kSmallSort);
+        uint16_t *sp = reinterpret_cast<uint16_t *>(si + kSmallSort);
+        uint32_t n2 = 1;
+        while (n2 < m) n2 <<= 1;
+        for (uint32_t k = tid; k < n2; k += kRB) {
+            if (k < m) {
+                sk[k] = (unsigned long long)__double_as_longlong(dist[k]);
+                si[k] = idx[k];
+                sp[k] = (uint16_t)k;
+            } else {
+                sk[k] = ~0ull;
+                si[k] = kNone;
+                sp[k] = 0xffff;
+            }
+        }
+        __syncthreads();
+        for (uint32_t size = 2; size <= n2; size <<= 1) {
+            for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+                for (uint32_t k = tid; k < n2; k += kRB) {
+                    const uint32_t j = k ^ stride;
+                    if (j > k) {
+                        const bool up = (k & size) == 0;
+                        const bool gt = sk[k] > sk[j] || (sk[k] == sk[j] && sp[k] > sp[j]);
+                        if (gt == up) {
+                            const unsigned long long tk = sk[k]; sk[k] = sk[j]; sk[j] = tk;
+                            const uint32_t ti = si[k]; si[k] = si[j]; si[j] = ti;
+                            const uint16_t tp = sp[k]; sp[k] = sp[j]; sp[j] = tp;
+                        }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        // (every size: below 17 members the library's insertion sort is stable by distance,
+        // which an order by squared distance only equals when no two roots tie)
+        int tie = 0;
+        for (uint32_t k = tid + 1; k < m; k += kRB)
+            tie |= rb_sqrt_tie(__longlong_as_double((long long)sk[k - 1]), __longlong_as_double((long long)sk[k]));
+        if (__syncthreads_or(tie)) {
+            if (tid == 0) s_tie = 1;
+        } else {
+            for (uint32_t k = tid; k < m; k += kRB) {
+                idx[k] = si[k];
+                dist[k] = __longlong_as_double((long long)sk[k]);
+            }
+        }
+        __syncthreads();
+    } else {
+        // 3b) large: radix sort of the top 32 bits with the position as payload into three
+        // fresh pool areas (D: the sorted segment; X, Y: sort buffers, given back after)
+        if (tid == 0) s_r = pool_try_alloc(a.P, 3 * m);
+        __syncthreads();
+        const uint32_t r = s_r;
+        if (r == kNone) {
+            ok = false;
+        } else {
+            uint32_t *kx = a.P.idx + r + m, *ky = a.P.idx + r + 2 * m;
+            uint32_t *vx = reinterpret_cast<uint32_t *>(a.P.dist + r + m), *vy = reinterpret_cast<uint32_t *>(a.P.dist + r + 2 * m);
+            for (uint32_t k = tid; k < m; k += kRB) {
+                kx[k] = (uint32_t)((unsigned long long)__double_as_longlong(dist[k]) >> 32);
+                vx[k] = k;
+            }
+            __syncthreads();
+            const int where = rb_radix32(kx, vx, ky, vy, m, reinterpret_cast<uint32_t *>(sh.buf));
+            const uint32_t *ks = where ? ky : kx, *vs = where ? vy : vx;
+            uint32_t *didx = a.P.idx + r;
+            double *ddist = a.P.dist + r;
+            for (uint32_t k = tid; k < m; k += kRB) {
+                const uint32_t src = vs[k];
+                didx[k] = idx[src];
+                ddist[k] = dist[src];
+            }
+            __syncthreads();
+            // runs of equal top bits: insertion sort by the full squared distance (stable)
+            for (uint32_t k = tid; k < m; k += kRB) {
+                if ((k == 0 || ks[k] != ks[k - 1]) && k + 1 < m && ks[k + 1] == ks[k]) {
+                    uint32_t e = k + 1;
+                    while (e < m && ks[e] == ks[k]) ++e;
+                    for (uint32_t i = k + 1; i < e; ++i) {
+                        const double dv = ddist[i];
+                        const uint32_t iv = didx[i];
+                        uint32_t j = i;
+                        while (j > k && ddist[j - 1] > dv) {
+                            ddist[j] = ddist[j - 1];
+                            didx[j] = didx[j - 1];
+                            --j;
+                        }
+                        ddist[j] = dv;
+                        didx[j] = iv;
+                    }
+                }
+            }
+            __syncthreads();
+            int tie = 0;
+            for (uint32_t k = tid + 1; k < m; k += kRB) tie |= rb_sqrt_tie(ddist[k - 1], ddist[k]);
+            if (__syncthreads_or(tie)) {
+                if (tid == 0) s_tie = 1;  // the unsorted segment at o is intact
+            } else if (tid == 0) {
+                a.ct.moff[slot] = r;
+            }
+            if (tid == 0) atomicCAS(a.P.top, r + 3 * m, r + m);  // give X and Y back when they are on top
+            __syncthreads();
+        }
+    }
+    if (ok && s_tie) {
+        // two members at the same distance: the library's std::sort order on the sequence
+        // before the sort, with the distances themselves (lib_sort.cuh, one thread)
+        for (uint32_t k = tid; k < m; k += kRB) dist[k] = sqrt(dist[k]);
+        __syncthreads();
+        if (tid == 0) lib_sort(dist, idx, m);
+        __syncthreads();
+    }
+    if (tid == 0) {
+        if (ok) {
+            a.needsort[slot] = 0;
+            a.distsq[slot] = s_tie ? 0 : 1;
+        } else {
+            a.needsort[slot] = 1;
+        }
+        if (stat) {
+            stat[5] += (unsigned long long)(clock64() - t0);
+            stat[6] += (unsigned long long)(t1 - t0);
+            stat[7] += 1;
+        }
+    }
+    __syncthreads();
+    return ok;
+}
+
+// ------------------------------------------------------------------ the persistent loop
+__global__ void __launch_bounds__(kRB, 2) k_rebind_loop(RbArgs a) {
+    __shared__ __align__(16) unsigned char buf[kFront * (3 * 4 + 2)];
+    __shared__ uint32_t warp_tot[kRB / 32];
+    __shared__ uint32_t u[16];
+    __shared__ double st[8], tabM[32], tabY[32];
+    __shared__ float tabF[32];
+    __shared__ uint32_t s_item;
+    RbShared sh{buf, warp_tot, u, st, tabM, tabY, tabF};
+    const int tid = threadIdx.x;
+    static_assert(kTile * (64 + 52 + 4 + 1) <= kFront * 14, "acceptance tile");
+    static_assert(7 * kKinTile * 8 <= kFront * 14, "sum tile");
+    static_assert(kSmallSort * 14 <= kFront * 14, "small sort");
+    static_assert((256 + 256 * (kRB / 32) + 1) * 4 <= kFront * 14, "radix counters");
+    for (uint32_t guard = 0; guard <= a.n; ++guard) {
+        if (tid == 0) s_item = atomicAdd(a.head, 1u);
+        __syncthreads();
+        const uint32_t item = s_item;
+        __syncthreads();
+        if (item >= a.n) return;
+        const uint32_t slot = a.list[item];
+        if (tid == 0 && a.blk_off) {
+            for (uint32_t b = a.blk_off[item]; b < a.blk_off[item + 1]; ++b) {
+                const uint32_t bs = a.blk[b];
+                for (uint32_t it = 0; *(volatile uint8_t *)&a.finished[bs] == 0; ++it) {
+                    if (it >= kWaitLimit) {
+                        atomicOr(a.err, (unsigned)kDevErrLoopLimit);
+                        break;
+                    }
+                    __nanosleep(1000);
+                }
+            }
+            __threadfence();
+        }
+        __syncthreads();
+        const uint32_t myrank = a.rank_of[slot];
+        unsigned long long *stat = a.stats ? a.stats + 8 * (size_t)slot : nullptr;
+        bool suspend = false;
+        if (a.needsort[slot]) suspend = !rb_sort_particles(a, slot, sh, stat);
+        for (uint32_t call = 0; !suspend; ++call) {
+            if (call >= kCallLimit) {
+                if (tid == 0) atomicOr(a.err, (unsigned)kDevErrLoopLimit);
+                break;
+            }
+            const uint32_t nacc = rb_call(a, slot, myrank, sh, stat);
+            if (nacc == kNone) {
+                suspend = true;
+                break;
+            }
+            if (nacc == 0) break;  // no growth: the Hill radius of the unchanged mass stays
+            if (!rb_sort_particles(a, slot, sh, stat)) suspend = true;
+        }
+        if (!suspend && a.distsq[slot]) {  // the distances of the last sort
+            const uint32_t o = a.ct.moff[slot], m = a.ct.mn[slot];
+            for (uint32_t k = tid; k < m; k += kRB) a.P.dist[o + k] = sqrt(a.P.dist[o + k]);
+            __syncthreads();
+            if (tid == 0) a.distsq[slot] = 0;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            a.suspended[slot] = suspend ? 1 : 0;
+            __threadfence();
+            *(volatile uint8_t *)&a.finished[slot] = 1;
+        }
+        __syncthreads();
+    }
+}

@@ -13,10 +13,7 @@ import cases
 from conftest import run_isolated
 from test_gpu_parity import check_cli_drop_in, check_stages_and_catalogue
 
-# Not yet run on a GPU: until a GPU run has passed them, a failure is
-# reported as XFAIL (and does not stop the suite before the tests that have passed); a pass
-# is reported as XPASS, which is their validation.
-pytestmark = [pytest.mark.gpu, pytest.mark.xfail(reason="not yet run on a GPU", strict=False)]
+pytestmark = pytest.mark.gpu
 
 SPLINE = [c.name for c in cases.SPLINE]
 

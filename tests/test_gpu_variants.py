@@ -17,10 +17,7 @@ import pytest
 import cases
 from conftest import GOLDEN, ROOT, golden, run_isolated
 
-# Not yet run on a GPU: until a GPU run has passed them, a failure is
-# reported as XFAIL (and does not stop the suite before the tests that have passed); a pass
-# is reported as XPASS, which is their validation.
-pytestmark = [pytest.mark.gpu, pytest.mark.xfail(reason="not yet run on a GPU", strict=False)]
+pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("name,case,extra", cases.VARIANTS, ids=[v[0] for v in cases.VARIANTS])

@@ -19,10 +19,7 @@ import pytest
 
 from conftest import GOLDEN, golden, run_isolated
 
-# Not yet run on a GPU: until a GPU run has passed them, a failure is
-# reported as XFAIL (and does not stop the suite before the tests that have passed); a pass
-# is reported as XPASS, which is their validation.
-pytestmark = [pytest.mark.gpu, pytest.mark.xfail(reason="not yet run on a GPU", strict=False)]
+pytestmark = pytest.mark.gpu
 
 MIX = ["w1_20k", "w1_20k_sinks", "w1_20k_border", "w1_24k_split2", "w2_250k", "w1_20k_spline80"]
 
@@ -31,7 +28,7 @@ def _check(pg, name, cat, tmp_path):
     g = golden(name)
     assert cat.summary().strip() == g["summary"], name
     d = tmp_path / name
-    d.mkdir()
+    d.mkdir(parents=True)
     cat.write_peaks(str(d / "res.txt"))
     assert (d / g["peaks_file"]).read_bytes() == (GOLDEN / name / g["peaks_file"]).read_bytes(), name
 
