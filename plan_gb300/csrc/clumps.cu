@@ -906,25 +906,53 @@ __device__ __forceinline__ int bound_hilo(const CandF &c, float Mf, const float 
     return -1;
 }
 
+// The same test with the FP32 quotient and square root taken by the fast intrinsics
+// (__fdividef, rsqrtf: at most 2 ulp each for the argument ranges admitted above). With
+// them A and B still carry a relative error below 2^-20, inside the margin.
+__device__ __forceinline__ int bound_hilo_fast(const CandF &c, float Mf, const float sh[6], const float sl[6], float G, float shear) {
+    const float dx = (sh[0] - c.ph[0]) + (sl[0] - c.pl[0]);
+    const float dy = (sh[1] - c.ph[1]) + (sl[1] - c.pl[1]);
+    const float dz = (sh[2] - c.ph[2]) + (sl[2] - c.pl[2]);
+    const float ex = (sh[3] - c.vh[0]) + (sl[3] - c.vl[0]);
+    const float t1 = (sh[4] - c.vh[1]) + (sl[4] - c.vl[1]), t2 = shear * dx;
+    const float ey = t1 - t2;
+    const float ez = (sh[5] - c.vh[2]) + (sl[5] - c.vl[2]);
+    const float K = ex * ex + ey * ey + ez * ez, D2 = dx * dx + dy * dy + dz * dz;
+    const float M = Mf + c.w;
+    if (!(K > 1e-30f && D2 > 1e-30f && K < 1e30f && D2 < 1e30f && M > 1e-30f && M < 1e30f)) return -1;
+    const float rM = __fdividef(1.0f, M);
+    const float A = 0.5f * rM * K, B = G * rsqrtf(D2);
+    const float e = A - B;
+    const float margin = (fabsf(A) + fabsf(B)) * 3.814697265625e-06f              // 2^-18
+                         + fabsf(ey) * (fabsf(t1) + fabsf(t2)) * 9.5367431640625e-07f * rM;  // 2^-20 / M
+    if (e > margin) return 0;
+    if (e < -margin) return 1;
+    return -1;
+}
+
 __device__ __forceinline__ void split_f(double d, float &hi, float &lo) {
     hi = (float)d;
     lo = (float)(d - (double)hi);
 }
 
 // Deferral records of a clump: the key ranks of the earlier clumps whose particles it
-// skipped (at most kDeferSlots distinct ranks; beyond that only the largest is known and
-// the host falls back to it).
+// skipped (at most kDeferSlots distinct records; beyond that only the largest rank is known
+// and the host falls back to it). A record carries kDeferSpec when the earlier clump had not
+// finished its calls when it was observed (its holding could still change in that pass);
+// without the bit the clump saw that pass's final holding.
 constexpr int kDeferSlots = 8;
+constexpr uint32_t kDeferSpec = 0x80000000u;
 
-__device__ void defer_add(uint32_t *dset, uint8_t *dover, uint32_t *dmax, uint32_t slot, uint32_t ow) {
+__device__ void defer_add(uint32_t *dset, uint8_t *dover, uint32_t *dmax, uint32_t slot, uint32_t ow, bool spec = true) {
     atomicMax(&dmax[slot], ow + 1);
+    const uint32_t rec = ow | (spec ? kDeferSpec : 0u);
     uint32_t *d = dset + (size_t)slot * kDeferSlots;
     for (int j = 0; j < kDeferSlots; ++j) {
         const uint32_t v = d[j];  // a set entry never changes again
-        if (v == ow) return;
+        if (v == rec) return;
         if (v == kNone) {
-            const uint32_t old = atomicCAS(&d[j], kNone, ow);
-            if (old == kNone || old == ow) return;
+            const uint32_t old = atomicCAS(&d[j], kNone, rec);
+            if (old == kNone || old == rec) return;
         }
     }
     dover[slot] = 1;
@@ -2301,7 +2329,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
         const bool use_rounds = rounds_env && *rounds_env == '1';
         uint8_t *d_fin = A.get<uint8_t>(nb), *d_susp = A.get<uint8_t>(nb), *d_needsort = A.get<uint8_t>(nb), *d_distsq = A.get<uint8_t>(nb);
         uint32_t *d_head = A.get<uint32_t>(4), *d_blkoff = A.get<uint32_t>(nb + 1);
-        unsigned long long *d_rstats = trace.on ? A.get<unsigned long long>(8 * nb) : nullptr;
+        unsigned long long *d_rstats = trace.on ? A.get<unsigned long long>((size_t)kRbStats * nb) : nullptr;
         double4_32a *tm0 = use_rounds ? nullptr : A.get<double4_32a>(Tu), *tm1 = use_rounds ? nullptr : A.get<double4_32a>(Tu);
         if (A.failed) return kErrOutOfMemory;
         int rb_grid = 1;
@@ -2310,11 +2338,11 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
             c.launches++;
             PLAN_CUDA(cudaMemsetAsync(d_needsort, 0, nb, s));
             PLAN_CUDA(cudaMemsetAsync(d_distsq, 0, nb, s));
-            if (d_rstats) PLAN_CUDA(cudaMemsetAsync(d_rstats, 0, 8 * nb * 8, s));
+            PLAN_CUDA(cudaFuncSetAttribute(k_rebind_loop, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRbSmem));
             int dev = 0, nsm = 0, per = 0;
             PLAN_CUDA(cudaGetDevice(&dev));
             PLAN_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-            PLAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rebind_loop, kRB, 0));
+            PLAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rebind_loop, kRB, kRbSmem));
             rb_grid = std::max(1, nsm * std::max(1, per));
         }
         uint64_t loop_launches = 0, suspensions = 0;
@@ -2370,6 +2398,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                 ra.epos = epos;
                 ra.owner = owner;
                 ra.rank_of = rank_of;
+                ra.slot_of_rank = slot_of_rank;
                 ra.tent = tent;
                 ra.dmax = dmax;
                 ra.dset = dset;
@@ -2380,7 +2409,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                 ra.err = c.d_err;
                 const unsigned grid = (unsigned)std::min<size_t>(todo.size(), (size_t)rb_grid);
                 double t_a = wall_ms();
-                k_rebind_loop<<<grid, kRB, 0, s>>>(ra);
+                k_rebind_loop<<<grid, kRB, kRbSmem, s>>>(ra);
                 c.launches++;
                 ++loop_launches;
                 PLAN_CUDA(cudaGetLastError());
@@ -2555,25 +2584,29 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
             } else {
                 // reruns wait on the device for the lower-ranked reruns they met in the last
                 // pass (PLAN_RERUN_SCHEDULE=0: all start at once)
+                if (d_rstats) PLAN_CUDA(cudaMemsetAsync(d_rstats, 0, (size_t)kRbStats * nb * 8, s));
                 rc = run_loop(active_all, (pass > 0 && !(sched_env && *sched_env == '0')) ? &blockers : nullptr);
                 if (!rc && trace.on) {
                     std::vector<unsigned long long> rs;
-                    rc = st.down(rs, d_rstats, 8 * nb);
+                    rc = st.down(rs, d_rstats, (size_t)kRbStats * nb);
                     if (!rc) {
                         size_t worst = 0;
                         unsigned long long wt = 0, calls = 0, acc = 0;
                         for (uint32_t sl : active_all) {
-                            const unsigned long long *q = &rs[8 * (size_t)sl];
+                            const unsigned long long *q = &rs[(size_t)kRbStats * sl];
                             calls += q[0];
                             acc += q[2];
                             if (q[3] + q[4] + q[5] > wt) { wt = q[3] + q[4] + q[5]; worst = sl; }
                         }
-                        const unsigned long long *w = &rs[8 * worst];
+                        const unsigned long long *w = &rs[(size_t)kRbStats * worst];
                         std::fprintf(stderr,
-                                     "[plan]   loop pass %u: %zu clumps, %llu calls, %llu accepted (cumulative); worst clump: calls %llu cand %llu acc %llu "
-                                     "kcycles search %llu accept %llu sort %llu (sums+dist %llu) sorts %llu\n",
-                                     (unsigned)pass, active_all.size(), calls, acc, w[0], w[1], w[2], w[3] / 1000, w[4] / 1000, w[5] / 1000,
-                                     w[6] / 1000, w[7]);
+                                     "[plan]   loop pass %u: %zu clumps, %llu calls, %llu accepted; worst clump: calls %llu scanned %llu cand %llu acc %llu "
+                                     "rounds %llu unsure %llu | kcycles search %llu accept %llu (warp-0 updates %llu: table %llu chain %llu) sort %llu (sums %llu; dist %llu "
+                                     "order %llu) sorts %llu members %llu | sum steps/kcycles:",
+                                     (unsigned)pass, active_all.size(), calls, acc, w[0], w[13], w[1], w[2], w[12], w[10], w[3] / 1000, w[4] / 1000,
+                                     w[14] / 1000, w[15] / 1000, w[16] / 1000, w[5] / 1000, w[6] / 1000, w[8] / 1000, w[9] / 1000, w[7], w[11]);
+                        for (int q = 0; q < 7; ++q) std::fprintf(stderr, " %llu/%llu", w[17 + q], w[24 + q] / 1000);
+                        std::fprintf(stderr, "\n");
                     }
                 }
             }
@@ -2618,8 +2651,13 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                     again = low != kNone && dm[sl] && dm[sl] - 1 >= low;
                 } else if (!again) {
                     for (int j = 0; j < kDeferSlots && !again; ++j) {
-                        const uint32_t d = ds[(size_t)sl * kDeferSlots + j];
-                        again = d != kNone && d < nlive && (rr[d] || changed[d]);
+                        const uint32_t d0 = ds[(size_t)sl * kDeferSlots + j];
+                        if (d0 == kNone) continue;
+                        // a partner that reruns; or one whose members differ from what this clump
+                        // assumed (it saw a holding that could still change)
+                        const uint32_t d = d0 & ~kDeferSpec;
+                        const bool spec = use_rounds || (d0 & kDeferSpec) != 0;
+                        again = d < nlive && (rr[d] || (spec && changed[d]));
                     }
                 }
                 if (again) { rerun.push_back(sl); rr[r] = 1; }
@@ -2636,8 +2674,8 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                     bool ready = true;
                     if (!dov[sl]) {
                         for (int j = 0; j < kDeferSlots && ready; ++j) {
-                            const uint32_t d = ds[(size_t)sl * kDeferSlots + j];
-                            ready = !(d != kNone && d < nlive && rr[d] && live[d] != sl);
+                            const uint32_t d0 = ds[(size_t)sl * kDeferSlots + j], d = d0 & ~kDeferSpec;
+                            ready = !(d0 != kNone && d < nlive && rr[d] && live[d] != sl);
                         }
                     }
                     if (ready) front.push_back(sl);
@@ -2673,8 +2711,8 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                 blockers[sa].clear();
                 if (!dov[sa]) {
                     for (int j = 0; j < kDeferSlots; ++j) {
-                        const uint32_t d = ds[(size_t)sa * kDeferSlots + j];
-                        if (d != kNone && d < nlive && rr[d] && live[d] != sa) blockers[sa].push_back(live[d]);
+                        const uint32_t d0 = ds[(size_t)sa * kDeferSlots + j], d = d0 & ~kDeferSpec;
+                        if (d0 != kNone && d < nlive && rr[d] && live[d] != sa) blockers[sa].push_back(live[d]);
                     }
                 } else {
                     const double ra = __builtin_bit_cast(double, rb[sa]);

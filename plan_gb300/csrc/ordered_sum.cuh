@@ -83,11 +83,12 @@ __device__ inline double warp_ordered_sum(const double *x, uint32_t n, double s)
 // The same sum with the grid rounding of the terms and the result done in integer
 // arithmetic (grid_term, grid_value): no FP64 instruction except for the ordinary adds
 // that start a run or step over a tie, a binade change or an out-of-range running sum.
-__device__ inline double warp_ordered_sum_int(const double *x, uint32_t n, double s) {
+__device__ inline double warp_ordered_sum_int(const double *x, uint32_t n, double s, uint32_t *iters = nullptr) {
     const int lane = threadIdx.x & 31;
     const unsigned full = 0xffffffffu;
     uint32_t k = 0;
     while (k < n) {
+        if (iters) ++*iters;
         const long long bits = __double_as_longlong(s);
         const uint32_t ex = (uint32_t)((bits >> 52) & 0x7ff);
         if (ex <= 60 || ex >= 2000) {  // zero, tiny or huge: no grid, one ordinary add
@@ -122,6 +123,111 @@ __device__ inline double warp_ordered_sum_int(const double *x, uint32_t n, doubl
         const long long na = __shfl_sync(full, nn, a - 1);
         s = grid_value(na, ex);
         k += (uint32_t)a;
+    }
+    return s;
+}
+
+// The same sum over a window of 32*K terms held in registers, lane l holding terms
+// [l K, l K + K) of the window in order (cnt valid terms). Each step rounds every
+// remaining term onto the grid of the running sum's binade, forms the integer prefix
+// sums lane by lane and then across the warp, and keeps the longest leading run whose
+// partial sums stay inside the binade (or reach its upper edge, which ends the run); the
+// first term that does not fit is added as one ordinary FP64 add. The step then continues
+// with the remaining terms of the same registers, so a binade change costs one step, not a
+// reload. Every lane returns the same value.
+template <int K>
+__device__ inline double warp_ordered_sum_window(const double (&x)[K], uint32_t cnt, double s, uint32_t *iters = nullptr) {
+    const int lane = threadIdx.x & 31;
+    const unsigned full = 0xffffffffu;
+    uint32_t pos = 0;  // terms of the window already added
+    while (pos < cnt) {
+        if (iters) ++*iters;
+        const long long bits = __double_as_longlong(s);
+        const uint32_t ex = (uint32_t)((bits >> 52) & 0x7ff);
+        if (bits == 0) {
+            // s = +0: adding a zero of either sign leaves +0, so a run of zero terms (particles
+            // at rest, say) is skipped at once; the first nonzero one is an ordinary add below
+            int fz = K;
+#pragma unroll
+            for (int j = 0; j < K; ++j) {
+                const uint32_t seq = (uint32_t)(lane * K + j);
+                if (fz == K && seq >= pos && seq < cnt && (__double_as_longlong(x[j]) << 1) != 0) fz = j;
+            }
+            const unsigned nz = __ballot_sync(full, fz < K);
+            if (!nz) break;  // only zeros remain
+            const int Lz = __ffs(nz) - 1;
+            pos = (uint32_t)(Lz * K + __shfl_sync(full, fz, Lz));
+        }
+        // this lane's remaining terms on the grid, and their prefix sums within the lane
+        long long t[K];
+        bool ok[K];
+        long long tot = 0;
+        const bool grid = ex > 60 && ex < 2000;
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            const uint32_t seq = (uint32_t)(lane * K + j);
+            const bool rem = seq >= pos && seq < cnt;
+            t[j] = 0;
+            ok[j] = true;
+            if (rem && grid) ok[j] = grid_term(x[j], ex, t[j]);
+            tot += t[j];
+        }
+        long long before = tot;  // inclusive scan across lanes, then exclusive
+        for (int d = 1; d < 32; d <<= 1) {
+            const long long v = __shfl_up_sync(full, before, d);
+            if (lane >= d) before += v;
+        }
+        before -= tot;
+        const long long mag = (bits & 0xfffffffffffffLL) | (1LL << 52);
+        const long long n0 = bits < 0 ? -mag : mag;  // s / u
+        // the first remaining term of this lane whose partial sum leaves the binade (stop at
+        // it) or lands on its upper edge (stop after it)
+        int stop = K;
+        bool stopped = false;
+        long long run = n0 + before;
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            const uint32_t seq = (uint32_t)(lane * K + j);
+            const bool rem = seq >= pos && seq < cnt;
+            if (rem && !stopped) {
+                run += t[j];
+                const long long an = run < 0 ? -run : run;
+                const bool inside = grid && ok[j] && ((run < 0) == (n0 < 0)) && an > (1LL << 52) && an <= (1LL << 53);
+                if (!inside) {
+                    stop = j;
+                    stopped = true;
+                } else if (an == (1LL << 53)) {
+                    stop = j + 1;
+                    stopped = true;
+                }
+            }
+        }
+        const unsigned hit = __ballot_sync(full, stopped);
+        const int L = hit ? __ffs(hit) - 1 : 31;
+        const int stopL = __shfl_sync(full, stop, L);
+        const uint32_t end = min(cnt, (uint32_t)(L * K + stopL));  // terms [pos, end) fit the grid
+        if (end > pos) {
+            // the grid integer of the partial sum after term end - 1
+            const uint32_t last = end - 1, ll = last / K;
+            long long val = n0 + before;
+#pragma unroll
+            for (int j = 0; j < K; ++j) {
+                const uint32_t seq = (uint32_t)(lane * K + j);
+                if (seq >= pos && seq <= last) val += t[j];
+            }
+            val = __shfl_sync(full, val, (int)ll);
+            s = grid_value(val, ex);
+            pos = end;
+        } else {
+            // the first remaining term does not fit the grid: one ordinary add
+            double v = 0.0;
+#pragma unroll
+            for (int j = 0; j < K; ++j)
+                if ((uint32_t)(lane * K + j) == pos) v = x[j];
+            v = __shfl_sync(full, v, (int)(pos / K));
+            s = s + v;
+            ++pos;
+        }
     }
     return s;
 }

@@ -4,36 +4,49 @@
 //     do { SearchBoundParticlesWithinHillRadius; CalculateHillRadius; } while (it grew)
 // where a call that accepts anything ends with SortParticles (src/tree.hpp:4678-4711,
 // 4446-4512, 4715-4717). k_rebind_loop runs that whole loop for a clump inside one block:
-// a persistent grid takes clumps from a queue in key-rank order, so a host round trip is
-// needed only per pass, not per call. Clumps of one launch run concurrently under the
-// ordered-claim rule of the round kernel (owner / tent / defer records); a clump may first
-// wait for lower-ranked clumps it met in the previous pass (its blockers). Those were taken
-// from the queue before it by running blocks, so every wait ends; each wait is bounded all
-// the same and reports kDevErrLoopLimit if it runs out.
+// a persistent grid (one 512-thread block per SM) takes clumps from a queue in key-rank
+// order, so the host is involved once per pass, not once per call. Clumps of one launch run
+// concurrently under the ordered-claim rule of the round kernel (owner / tent / defer
+// records); a clump may first wait for the lower-ranked clumps it met in the previous pass
+// (its blockers). Those were taken from the queue before it by running blocks, so every
+// wait ends; each wait is bounded all the same and reports kDevErrLoopLimit if it runs out.
 //
-// Inside a call:
+// On this GPU an FP64 instruction holds the SM's FP64 pipe for ~19 cycles whatever the
+// number of active lanes, and a dependent one waits 36-55 cycles (a division ~590, a square
+// root ~630), so the loop keeps FP64 work off its chains:
 //  * ball search: the breadth-first frontier of the round kernel, then one block-wide pass
 //    over the eligible points of every frontier entry (a contained node keeps all of them,
 //    a boundary node keeps those in the ball), compacted in point order;
-//  * acceptance: warp 0 tests 32 staged candidates at a time in FP32 (FP64 when too close
-//    to call) and takes the first bound one. The state update is the reference's FP64
-//    formula; its division is a reciprocal product with Markstein's correction, the
-//    reciprocals of the next masses taken 32 at a time off the dependent chain while all
-//    accepted particles have the same mass;
-//  * SortParticles: the seven member sums in member order (warp_ordered_sum_int over
-//    per-point products m, m x, ..., m vz formed once per snapshot), the centre of mass and
-//    the Hill radius, squared distances, and a stable sort by squared distance (in shared
-//    memory up to kSmallSort members, else a block radix sort on the top 32 bits followed
-//    by an exact fix-up of equal prefixes). Squared distances order members as distances
-//    do, except that two squared distances may round to one distance: neighbours within a
-//    few ulps are compared through their square roots, and a tie goes to the library-order
-//    replay exactly as in the round kernels. The square roots of the last sort are taken
-//    when the clump's loop ends.
+//  * acceptance: 512 candidates at a time, one per thread in registers (the next 512
+//    prefetched meanwhile). Every thread tests its candidate against the current state in
+//    FP32 (FP64 when too close to call), the block finds the first bound one, and warp 0
+//    applies the reference's FP64 update to the state. Its division is a reciprocal product
+//    with Markstein's correction; the reciprocals of the next masses are taken 32 at a time
+//    off the dependent chain while the accepted particles have equal masses;
+//  * SortParticles: the seven member sums in member order (warp_ordered_sum_window over
+//    per-point products m, m x, ..., m vz formed once per snapshot, 128 terms per step with
+//    the next terms prefetched into registers), the centre of mass and the Hill radius,
+//    squared distances, and a stable sort by squared distance (in shared memory up to
+//    kRbSmall members, else a block radix sort on the top 32 bits and an exact fix-up of
+//    equal prefixes). Squared distances order members as distances do, except that two
+//    squared distances may round to one distance: neighbours within a few ulps are compared
+//    through their square roots, and a tie goes to the library-order replay exactly as in
+//    the round kernels. The square roots of the last sort are taken when the loop ends.
 #pragma once
 
-constexpr int kRB = 256;                      // threads of a rebinding block
+constexpr int kRB = 512;                      // threads of a rebinding block
+constexpr int kRbWarps = kRB / 32;
+constexpr uint32_t kRbFront = 4096;           // frontier entries of the ball search
+constexpr uint32_t kRbSmall = 4096;           // members sorted in shared memory
 constexpr uint32_t kWaitLimit = 1u << 25;     // bounded waits on blockers (about 30 s)
 constexpr uint32_t kCallLimit = 1u << 20;     // calls of one clump in one launch
+constexpr int kRbStats = 32;                  // counters per slot
+// dynamic shared memory: the largest phase is the frontier / the small sort
+constexpr size_t kRbSmem = 14 * (kRbFront > kRbSmall ? kRbFront : kRbSmall);
+static_assert(kRbFront * 14 <= kRbSmem, "frontier");
+static_assert((size_t)kRB * 68 <= kRbSmem, "acceptance tile");
+static_assert(kRbSmall * 14 <= kRbSmem, "small sort");
+static_assert((256 + 256 * kRbWarps + 1) * 4 <= kRbSmem, "radix counters");
 
 struct RbArgs {
     const uint32_t *list;  // clumps of this launch, in key-rank order
@@ -44,7 +57,7 @@ struct RbArgs {
     uint8_t *suspended;    // per slot: stopped because the member pool is full (state consistent)
     uint8_t *needsort;     // per slot: the last call grew the clump but its SortParticles is pending
     uint8_t *distsq;       // per slot: the segment's distances are still squared
-    unsigned long long *stats;  // per slot, 8 counters (may be null)
+    unsigned long long *stats;  // per slot, kRbStats counters (may be null)
     CT ct;
     Pool P;
     KTree t;
@@ -53,7 +66,7 @@ struct RbArgs {
     const double4_32a *tm0, *tm1;  // per point: (m, m x, m y, m z), (m vx, m vy, m vz, 0)
     const uint32_t *E, *epos;
     uint32_t *owner;
-    const uint32_t *rank_of, *tent;
+    const uint32_t *rank_of, *slot_of_rank, *tent;
     uint32_t *dmax, *dset;
     uint8_t *dover;
     const double4_32a *com0;
@@ -83,7 +96,7 @@ __device__ __forceinline__ uint32_t rb_block_rank(bool keep, uint32_t &rank, uin
     if (lane == 0) warp_tot[wid] = __popc(b);
     __syncthreads();
     uint32_t before = 0, total = 0;
-    for (int w = 0; w < kRB / 32; ++w) {
+    for (int w = 0; w < kRbWarps; ++w) {
         const uint32_t c = warp_tot[w];
         if (w < wid) before += c;
         total += c;
@@ -93,23 +106,54 @@ __device__ __forceinline__ uint32_t rb_block_rank(bool keep, uint32_t &rank, uin
     return total;
 }
 
+// exclusive scan of a[0, n) in shared memory by the whole block; returns the total
+__device__ uint32_t rb_scan_excl(uint32_t *a, uint32_t n, uint32_t *warp_tot) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t per = (n + kRB - 1) / kRB;
+    const uint32_t b = threadIdx.x * per, e = min(n, b + per);
+    uint32_t sum = 0;
+    for (uint32_t i = b; i < e; ++i) sum += a[i];
+    uint32_t incl = sum;
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += v;
+    }
+    if (lane == 31) warp_tot[wid] = incl;
+    __syncthreads();
+    uint32_t before = 0, total = 0;
+    for (int k = 0; k < kRbWarps; ++k) {
+        if (k < wid) before += warp_tot[k];
+        total += warp_tot[k];
+    }
+    uint32_t run = before + incl - sum;
+    for (uint32_t i = b; i < e; ++i) {
+        const uint32_t v = a[i];
+        a[i] = run;
+        run += v;
+    }
+    __syncthreads();
+    return total;
+}
+
 struct RbShared {
-    unsigned char *buf;  // kFront * 14 bytes, reused by every phase
+    unsigned char *buf;  // kRbSmem bytes, reused by every phase
     uint32_t *warp_tot;
     uint32_t *u;         // scalars
-    double *st;          // M, com x y z, vcom x y z, hill
-    double *tabM, *tabY;
+    double *st;          // M, com x y z, vcom x y z, hill (the call's starting state)
+    double *tabM, *tabY; // reciprocal table (warp 0)
     float *tabF;
+    float *sf;           // acceptance state for every thread: hi[6], lo[6], Mf
+    double *sd;          // acceptance state in FP64: x y z vx vy vz M
 };
 
 // ------------------------------------------------------------------ one SearchBound call
 // Returns the number of accepted particles, or kNone when the member pool is full (nothing
 // changed).
 __device__ uint32_t rb_call(const RbArgs &a, uint32_t slot, uint32_t myrank, RbShared &sh, unsigned long long *stat) {
-    const int tid = threadIdx.x, lane = tid & 31;
-    uint32_t *front = reinterpret_cast<uint32_t *>(sh.buf), *front2 = front + kFront, *fcnt = front2 + kFront;
-    uint8_t *fcls = reinterpret_cast<uint8_t *>(fcnt + kFront), *fcls2 = fcls + kFront;
-    uint32_t &s_nf = sh.u[0], &s_expand = sh.u[1], &s_noff = sh.u[2], &s_nel = sh.u[3], &s_nacc = sh.u[4], &s_m0 = sh.u[5],
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    uint32_t *front = reinterpret_cast<uint32_t *>(sh.buf), *front2 = front + kRbFront, *fcnt = front2 + kRbFront;
+    uint8_t *fcls = reinterpret_cast<uint8_t *>(fcnt + kRbFront), *fcls2 = fcls + kRbFront;
+    uint32_t &s_nf = sh.u[0], &s_expand = sh.u[1], &s_noff = sh.u[2], &s_nel = sh.u[3], &s_f = sh.u[4], &s_m0 = sh.u[5],
              &s_o = sh.u[6], &s_S = sh.u[7];
     const long long t0 = clock64();
     if (tid == 0) {
@@ -124,7 +168,6 @@ __device__ uint32_t rb_call(const RbArgs &a, uint32_t slot, uint32_t myrank, RbS
         fcls[0] = 0;
         s_nf = 1;
         s_nel = 0;
-        s_nacc = 0;
         const double4_32a c0 = a.com0[slot];  // how far this clump's balls reach from its centre before rebinding
         const double dx = c.x - c0.x, dy = c.y - c0.y, dz = c.z - c0.z;
         const double d = sqrt(dx * dx + dy * dy + dz * dz) + sh.st[7];
@@ -156,8 +199,8 @@ __device__ uint32_t rb_call(const RbArgs &a, uint32_t slot, uint32_t myrank, RbS
         }
         __syncthreads();
         if (!s_expand) break;
-        const uint32_t total = block_scan_excl(fcnt, nf, sh.warp_tot);
-        if (total > (uint32_t)kFront) break;
+        const uint32_t total = rb_scan_excl(fcnt, nf, sh.warp_tot);
+        if (total > kRbFront) break;
         for (uint32_t i = tid; i < nf; i += kRB) {
             const int cls = fcls[i];
             const uint32_t o = fcnt[i];
@@ -198,7 +241,7 @@ __device__ uint32_t rb_call(const RbArgs &a, uint32_t slot, uint32_t myrank, RbS
         fcnt[i] = cls == 3 ? 0u : ee - eb;
     }
     __syncthreads();
-    const uint32_t S = block_scan_excl(fcnt, nf, sh.warp_tot);
+    const uint32_t S = rb_scan_excl(fcnt, nf, sh.warp_tot);
     // 3) the new segment: the members, then room for every scanned point
     if (tid == 0) {
         s_S = S;
@@ -232,89 +275,134 @@ __device__ uint32_t rb_call(const RbArgs &a, uint32_t slot, uint32_t myrank, RbS
     }
     const uint32_t nel = s_nel;
     const long long t1 = clock64();
-    // 4) the reference's sequential acceptance (src/tree.hpp:4686-4706)
-    double4_32a *tpos = reinterpret_cast<double4_32a *>(sh.buf), *tvel = tpos + kTile;
-    CandF *tf = reinterpret_cast<CandF *>(tvel + kTile);
-    uint32_t *tq = reinterpret_cast<uint32_t *>(tf + kTile);
-    uint8_t *ttaken = reinterpret_cast<uint8_t *>(tq + kTile);
+    // 4) the reference's sequential acceptance (src/tree.hpp:4686-4706), 512 candidates at a
+    // time. Every thread holds one candidate: q, its FP32 form in registers, its FP64
+    // position and velocity in shared memory.
+    double4_32a *tpos = reinterpret_cast<double4_32a *>(sh.buf), *tvel = tpos + kRB;
+    uint32_t *tq = reinterpret_cast<uint32_t *>(tvel + kRB);
     const float G32 = (float)a.cp.G, shear32 = (float)a.cp.shear;
-    double M = 0, comp = 0;          // warp 0: the mass and, in lane c < 6, component c of the state
-    float Mf = 0.f, shv[6], slv[6];  // its float forms
-    double tab_m = -1.0;             // the mass the reciprocal table was built for
+    double comp = 0.0;      // warp 0, lane c < 6: component c of the state (x y z vx vy vz)
+    double M = sh.st[0];    // warp 0: the mass
+    double tab_m = -1.0;    // warp 0: the mass the reciprocal table was built for
     int tab_n = 0, tab_i = 0;
-    uint32_t nacc = 0;
+    uint32_t nacc = 0, rounds = 0;
+    if (tid == 0) {
+        sh.u[12] = 0;
+        sh.u[13] = 0;
+        sh.u[14] = 0;
+        sh.u[15] = 0;
+    }
     if (tid < 32) {
-        M = sh.st[0];
         comp = lane < 6 ? sh.st[1 + lane] : 0.0;
         float h = 0.f, l = 0.f;
         split_any(comp, h, l);
-        for (int c = 0; c < 6; ++c) {
-            shv[c] = __shfl_sync(0xffffffffu, h, c);
-            slv[c] = __shfl_sync(0xffffffffu, l, c);
+        if (lane < 6) {
+            sh.sf[lane] = h;
+            sh.sf[6 + lane] = l;
+            sh.sd[lane] = comp;
         }
-        float mh, ml;
-        split_any(M, mh, ml);
-        Mf = mh;
+        if (lane == 0) {
+            float mh, ml;
+            split_any(M, mh, ml);
+            sh.sf[12] = mh;
+            sh.sd[6] = M;
+        }
     }
-    for (uint32_t base = 0; base < nel; base += kTile) {
-        const uint32_t tend = min(nel, base + (uint32_t)kTile);
-        for (uint32_t i = tid; base + i < tend; i += kRB) {
-            const uint32_t q2 = elig[base + i];
-            const uint32_t ow = __ldcg(&a.owner[q2]), tn = a.tent[q2];
-            const bool taken = (ow != kNone && ow <= myrank) || (tn != kNone && tn < myrank);
-            if (ow != kNone && ow < myrank) defer_add(a.dset, a.dover, a.dmax, slot, ow);
-            else if (tn != kNone && tn < myrank) defer_add(a.dset, a.dover, a.dmax, slot, tn);
-            tq[i] = q2;
-            ttaken[i] = taken ? 1 : 0;
-            const double4_32a pp = t.pos[q2], vv = a.vel[q2];
-            tpos[i] = pp;
-            tvel[i] = vv;
-            const float4 ph = a.ft.phi[q2], pl = a.ft.plo[q2];
-            CandF cf;
-            cf.ph[0] = ph.x; cf.ph[1] = ph.y; cf.ph[2] = ph.z;
-            cf.pl[0] = pl.x; cf.pl[1] = pl.y; cf.pl[2] = pl.z;
-            split_any(vv.x, cf.vh[0], cf.vl[0]);
-            split_any(vv.y, cf.vh[1], cf.vl[1]);
-            split_any(vv.z, cf.vh[2], cf.vl[2]);
+    // the prefetched candidate of the next tile
+    uint32_t nq = kNone, now_ = kNone, ntn = kNone;
+    double4_32a np = make_double4_32a(0, 0, 0, 0), nv = make_double4_32a(0, 0, 0, 0);
+    float4 nph = make_float4(0.f, 0.f, 0.f, 0.f), npl = nph;
+    if ((uint32_t)tid < nel) {
+        nq = elig[tid];
+        now_ = __ldcg(&a.owner[nq]);
+        ntn = a.tent[nq];
+        np = t.pos[nq];
+        nv = a.vel[nq];
+        nph = a.ft.phi[nq];
+        npl = a.ft.plo[nq];
+    }
+    for (uint32_t base = 0; base < nel; base += kRB) {
+        const uint32_t q = nq;
+        const bool valid = q != kNone;
+        bool taken = true;
+        CandF cf;
+        if (valid) {
+            uint32_t ow = now_, tn = ntn;
+            if (tn != kNone && tn < myrank && *(volatile const uint8_t *)&a.finished[a.slot_of_rank[tn]]) {
+                // that clump has finished its calls in this launch: its claims are its
+                // holdings, and its prediction from the last pass no longer applies
+                __threadfence();
+                ow = __ldcg(&a.owner[q]);
+                tn = kNone;
+            }
+            taken = (ow != kNone && ow <= myrank) || (tn != kNone && tn < myrank);
+            if (ow != kNone && ow < myrank)
+                defer_add(a.dset, a.dover, a.dmax, slot, ow, *(volatile const uint8_t *)&a.finished[a.slot_of_rank[ow]] == 0);
+            else if (tn != kNone && tn < myrank)
+                defer_add(a.dset, a.dover, a.dmax, slot, tn, true);
+            tpos[tid] = np;
+            tvel[tid] = nv;
+            tq[tid] = q;
+            cf.ph[0] = nph.x; cf.ph[1] = nph.y; cf.ph[2] = nph.z;
+            cf.pl[0] = npl.x; cf.pl[1] = npl.y; cf.pl[2] = npl.z;
+            split_any(nv.x, cf.vh[0], cf.vl[0]);
+            split_any(nv.y, cf.vh[1], cf.vl[1]);
+            split_any(nv.z, cf.vh[2], cf.vl[2]);
             float wl;
-            split_any(pp.w, cf.w, wl);
-            tf[i] = cf;
+            split_any(np.w, cf.w, wl);
+        }
+        nq = kNone;
+        if (base + kRB + tid < nel) {  // prefetch (accepted ones are written below base + kRB only)
+            nq = elig[base + kRB + tid];
+            now_ = __ldcg(&a.owner[nq]);
+            ntn = a.tent[nq];
+            np = t.pos[nq];
+            nv = a.vel[nq];
+            nph = a.ft.phi[nq];
+            npl = a.ft.plo[nq];
         }
         __syncthreads();
-        if (tid < 32) {
-            const unsigned full = 0xffffffffu;
-            uint32_t at = base;
-            while (at < tend) {
-                const uint32_t k = at + lane;
-                bool bound = false, unsure = false;
-                if (k < tend && !ttaken[k - base]) {
-                    const int r = bound_hilo(tf[k - base], Mf, shv, slv, G32, shear32);
-                    if (r >= 0) bound = r == 1;
-                    else unsure = true;
+        for (uint32_t pos = 0;;) {
+            ++rounds;
+            bool bound = false, unsure = false;
+            if (valid && !taken && (uint32_t)tid >= pos) {
+                float shv[6], slv[6];
+                for (int c = 0; c < 6; ++c) {
+                    shv[c] = sh.sf[c];
+                    slv[c] = sh.sf[6 + c];
                 }
-                if (__any_sync(full, unsure)) {  // the FP64 test needs the whole state in every lane
-                    const double x = __shfl_sync(full, comp, 0), y = __shfl_sync(full, comp, 1), z = __shfl_sync(full, comp, 2);
-                    const double vx = __shfl_sync(full, comp, 3), vy = __shfl_sync(full, comp, 4), vz = __shfl_sync(full, comp, 5);
-                    if (unsure) bound = bound_fp64(tpos[k - base], tvel[k - base], M, x, y, z, vx, vy, vz, a.cp);
-                }
-                const unsigned b = __ballot_sync(full, bound);
-                if (!b) {
-                    at = min(at + 32, tend);
-                    continue;
-                }
-                const int f = __ffs(b) - 1;
-                const uint32_t j = at + f - base;
-                const double m = tpos[j].w;
-                if (!(tab_i < tab_n && m == tab_m)) {
-                    // the next masses M_{l+1} = RN(M_l + m) on the grid of M's binade (exact while
-                    // they stay inside it), and their correctly rounded reciprocals, one per lane
+                const int r = bound_hilo_fast(cf, sh.sf[12], shv, slv, G32, shear32);
+                if (r >= 0) bound = r == 1;
+                else unsure = true;
+            }
+            if (unsure) {
+                bound = bound_fp64(tpos[tid], tvel[tid], sh.sd[6], sh.sd[0], sh.sd[1], sh.sd[2], sh.sd[3], sh.sd[4], sh.sd[5], a.cp);
+                if (stat) atomicAdd(&sh.u[12], 1u);
+            }
+            const unsigned b = __ballot_sync(0xffffffffu, bound);
+            if (lane == 0) sh.warp_tot[wid] = b ? (uint32_t)(wid * 32 + __ffs(b) - 1) : kNone;
+            __syncthreads();
+            uint32_t f = kNone;
+            {
+                uint32_t wv[kRbWarps];
+                for (int w = 0; w < kRbWarps; ++w) wv[w] = sh.warp_tot[w];
+                for (int w = kRbWarps - 1; w >= 0; --w) f = wv[w] != kNone ? wv[w] : f;
+            }
+            if (f == kNone) break;  // the rest of the tile is not bound
+            if (tid < 32) {
+                const long long tu0 = clock64();
+                const unsigned full = 0xffffffffu;
+                const double m = tpos[f].w;
+                if (!(tab_i < tab_n && dbits(m) == dbits(tab_m))) {
+                    // the next masses M_{l+1} = RN(M_l + m) on the grid of M's binade (exact
+                    // while they stay inside it), and their correctly rounded reciprocals
                     tab_m = m;
                     tab_i = 0;
                     tab_n = 0;
                     const uint64_t mb = dbits(M);
                     const uint32_t ex = (uint32_t)(mb >> 52) & 0x7ffu;
                     long long dn = 0;
-                    if (M > 0.0 && m > 0.0 && ex > 60u && ex < 2000u && grid_term(m, ex, dn) && dn > 0) {
+                    if ((mb >> 63) == 0 && ex > 60u && ex < 2000u && grid_term(m, ex, dn) && dn > 0) {
                         const long long n0 = (long long)((mb & 0xfffffffffffffull) | (1ull << 52));
                         const long long nl = n0 + (long long)(lane + 1) * dn;
                         const bool ok = nl > (1LL << 52) && nl <= (1LL << 53);
@@ -334,6 +422,7 @@ __device__ uint32_t rb_call(const RbArgs &a, uint32_t slot, uint32_t myrank, RbS
                         __syncwarp();
                     }
                 }
+                const long long tu1 = clock64();
                 double Mn, y;
                 float Mnf;
                 if (tab_i < tab_n) {
@@ -350,40 +439,46 @@ __device__ uint32_t rb_call(const RbArgs &a, uint32_t slot, uint32_t myrank, RbS
                 }
                 // src/tree.hpp:4696-4701 (the new mass multiplies the old centre): lane c < 6
                 // updates component c as RN(RN(RN(c M') + RN(m q_c)) / M')
-                float h = 0.f, l = 0.f;
                 if (lane < 6) {
-                    const double4_32a p = tpos[j], v = tvel[j];
+                    const double4_32a p = tpos[f], v = tvel[f];
                     const double qc = lane == 0 ? p.x : lane == 1 ? p.y : lane == 2 ? p.z : lane == 3 ? v.x : lane == 4 ? v.y : v.z;
                     const double num = comp * Mn + m * qc;
-                    if (num == 0.0) {
+                    if ((dbits(num) << 1) == 0) {
                         comp = num;  // the quotient keeps the numerator's zero
                     } else {
                         const double q0 = num * y;
                         comp = fma(fma(-q0, Mn, num), y, q0);
                     }
+                    float h, l;
+                    if (stat && lane == 0) sh.u[15] += (uint32_t)(clock64() - tu1);
                     split_any(comp, h, l);
-                }
-                for (int c = 0; c < 6; ++c) {
-                    shv[c] = __shfl_sync(full, h, c);
-                    slv[c] = __shfl_sync(full, l, c);
+                    sh.sf[lane] = h;
+                    sh.sf[6 + lane] = l;
+                    sh.sd[lane] = comp;
                 }
                 M = Mn;
-                Mf = Mnf;
                 if (lane == 0) {
-                    const uint32_t q2 = tq[j];
+                    sh.sf[12] = Mnf;
+                    sh.sd[6] = Mn;
+                    const uint32_t q2 = tq[f];
                     // the lowest rank keeps the particle; who lost one is found after the pass
                     atomicMin(&a.owner[q2], myrank);
                     elig[nacc] = q2;  // accepted ones overwrite candidates already consumed
+                    if (stat) {
+                        sh.u[13] += (uint32_t)(clock64() - tu0);
+                        sh.u[14] += (uint32_t)(tu1 - tu0);
+                    }
                 }
                 ++nacc;
-                at += f + 1;
             }
+            __syncthreads();
+            pos = f + 1;
         }
         __syncthreads();
     }
-    if (tid == 0) s_nacc = nacc;
+    if (tid == 0) s_f = nacc;
     __syncthreads();
-    nacc = s_nacc;
+    nacc = s_f;
     const long long t2 = clock64();
     if (tid == 0) {
         if (stat) {
@@ -392,6 +487,12 @@ __device__ uint32_t rb_call(const RbArgs &a, uint32_t slot, uint32_t myrank, RbS
             stat[2] += nacc;
             stat[3] += (unsigned long long)(t1 - t0);
             stat[4] += (unsigned long long)(t2 - t1);
+            stat[12] += rounds;
+            stat[13] += S;
+            stat[10] += sh.u[12];
+            stat[14] += sh.u[13];
+            stat[15] += sh.u[14];  // of which the table look-up / rebuild
+            stat[16] += sh.u[15];  // and the FP64 update chain
         }
         if (nacc) {
             a.ct.moff[slot] = no;
@@ -410,13 +511,13 @@ __device__ uint32_t rb_call(const RbArgs &a, uint32_t slot, uint32_t myrank, RbS
 // the result is in (ki, vi), 1 when in (ko, vo).
 __device__ int rb_radix32(uint32_t *ki, uint32_t *vi, uint32_t *ko, uint32_t *vo, uint32_t n, uint32_t *smem) {
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    uint32_t *hist = smem, *wcnt = smem + 256, *flag = smem + 256 + 256 * (kRB / 32);
+    uint32_t *hist = smem, *wcnt = smem + 256, *flag = smem + 256 + 256 * kRbWarps;
     int where = 0;
     for (int pass = 0; pass < 4; ++pass) {
         const int sh = 8 * pass;
         uint32_t *kin = where ? ko : ki, *vin = where ? vo : vi, *kout = where ? ki : ko, *vout = where ? vi : vo;
         for (int d = tid; d < 256; d += kRB) hist[d] = 0;
-        for (int d = tid; d < 256 * (kRB / 32); d += kRB) wcnt[d] = 0;
+        for (int d = tid; d < 256 * kRbWarps; d += kRB) wcnt[d] = 0;
         if (tid == 0) flag[0] = 0;
         __syncthreads();
         for (uint32_t i = tid; i < n; i += kRB) atomicAdd(&hist[(kin[i] >> sh) & 255u], 1u);
@@ -455,7 +556,7 @@ __device__ int rb_radix32(uint32_t *ki, uint32_t *vi, uint32_t *ko, uint32_t *vo
             __syncthreads();
             for (int d = tid; d < 256; d += kRB) {
                 uint32_t tot = 0;
-                for (int w = 0; w < kRB / 32; ++w) {
+                for (int w = 0; w < kRbWarps; ++w) {
                     tot += wcnt[w * 256 + d];
                     wcnt[w * 256 + d] = 0;
                 }
@@ -491,27 +592,46 @@ __device__ bool rb_sort_particles(const RbArgs &a, uint32_t slot, RbShared &sh, 
     const uint32_t o = s_o, m = s_m;
     uint32_t *idx = a.P.idx + o;
     double *dist = a.P.dist + o;
-    // 1) the seven sums in member order (CalculateKinematicProperties)
-    double *term = reinterpret_cast<double *>(sh.buf);  // [7][kKinTile]
+    // 1) the seven sums in member order (CalculateKinematicProperties): warp w < 7 runs sum w
+    // over the per-point products, 128 terms per step; the member indices of the window
+    // after next and the terms of the next window are loaded while a window is summed
     double acc = 0.0;
-    for (uint32_t base = 0; base < m; base += kKinTile) {
-        const uint32_t cnt = min((uint32_t)kKinTile, m - base);
-        for (uint32_t i = tid; i < cnt; i += kRB) {
-            const uint32_t q = idx[base + i];
-            const double4_32a A = a.tm0[q], B = a.tm1[q];
-            term[0 * kKinTile + i] = A.x;
-            term[1 * kKinTile + i] = A.y;
-            term[2 * kKinTile + i] = A.z;
-            term[3 * kKinTile + i] = A.w;
-            term[4 * kKinTile + i] = B.x;
-            term[5 * kKinTile + i] = B.y;
-            term[6 * kKinTile + i] = B.z;
+    uint32_t its = 0;
+    long long tsum = 0;
+    if (wid < 7) {
+        const long long ts = clock64();
+        const double *tsrc = wid < 4 ? reinterpret_cast<const double *>(a.tm0) + wid : reinterpret_cast<const double *>(a.tm1) + (wid - 4);
+        constexpr int kK = 4;  // terms per lane and window
+        constexpr uint32_t kW = 32 * kK;
+        uint32_t qa[kK], qb[kK];
+        double x[kK], nx[kK];
+#pragma unroll
+        for (int j = 0; j < kK; ++j) {
+            const uint32_t k = (uint32_t)lane * kK + j;
+            qa[j] = k < m ? idx[k] : 0u;
+            qb[j] = kW + k < m ? idx[kW + k] : 0u;
         }
-        __syncthreads();
-        if (wid < 7) acc = warp_ordered_sum_int(term + wid * kKinTile, cnt, acc);
-        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < kK; ++j) x[j] = (uint32_t)lane * kK + j < m ? tsrc[4 * (size_t)qa[j]] : 0.0;
+        for (uint32_t base = 0; base < m; base += kW) {
+#pragma unroll
+            for (int j = 0; j < kK; ++j) {
+                const uint32_t k = base + kW + (uint32_t)lane * kK + j;
+                nx[j] = k < m ? tsrc[4 * (size_t)qb[j]] : 0.0;
+                const uint32_t k2 = k + kW;
+                qb[j] = k2 < m ? idx[k2] : 0u;
+            }
+            acc = warp_ordered_sum_window<kK>(x, min(kW, m - base), acc, &its);
+#pragma unroll
+            for (int j = 0; j < kK; ++j) x[j] = nx[j];
+        }
+        tsum = clock64() - ts;
     }
     if (wid < 7 && lane == 0) sh.tabM[wid] = acc;  // the table is free between calls
+    if (wid < 7 && lane == 0 && stat) {  // each sum: its time and its steps
+        atomicAdd(&stat[17 + wid], (unsigned long long)its);
+        atomicAdd(&stat[24 + wid], (unsigned long long)tsum);
+    }
     __syncthreads();
     if (tid < 32) {
         const double Ms = sh.tabM[0];
@@ -522,6 +642,7 @@ __device__ bool rb_sort_particles(const RbArgs &a, uint32_t slot, RbShared &sh, 
         if (lane == 0) sh.st[0] = Ms;
     }
     __syncthreads();
+    const long long t_sum = clock64();
     if (tid == 0) {
         a.ct.M[slot] = sh.st[0];
         a.ct.com[slot] = make_double4_32a(sh.st[1], sh.st[2], sh.st[3], 0);
@@ -539,13 +660,13 @@ __device__ bool rb_sort_particles(const RbArgs &a, uint32_t slot, RbShared &sh, 
         dist[k] = s;
     }
     __syncthreads();
-    const long long t1 = clock64();
+    const long long t_dist = clock64();
     bool ok = true;
-    if (m <= (uint32_t)kSmallSort) {
+    if (m <= kRbSmall) {
         // 3a) in shared memory: bitonic sort by (squared distance, position)
         unsigned long long *sk = reinterpret_cast<unsigned long long *>(sh.buf);
-        uint32_t *si = reinterpret_cast<uint32_t *>(sk + kSmallSort);
-        uint16_t *sp = reinterpret_cast<uint16_t *>(si + kSmallSort);
+        uint32_t *si = reinterpret_cast<uint32_t *>(sk + kRbSmall);
+        uint16_t *sp = reinterpret_cast<uint16_t *>(si + kRbSmall);
         uint32_t n2 = 1;
         while (n2 < m) n2 <<= 1;
         for (uint32_t k = tid; k < n2; k += kRB) {
@@ -664,9 +785,13 @@ __device__ bool rb_sort_particles(const RbArgs &a, uint32_t slot, RbShared &sh, 
             a.needsort[slot] = 1;
         }
         if (stat) {
-            stat[5] += (unsigned long long)(clock64() - t0);
-            stat[6] += (unsigned long long)(t1 - t0);
+            const long long t3 = clock64();
+            stat[5] += (unsigned long long)(t3 - t0);
+            stat[6] += (unsigned long long)(t_sum - t0);
             stat[7] += 1;
+            stat[8] += (unsigned long long)(t_dist - t_sum);
+            stat[9] += (unsigned long long)(t3 - t_dist);
+            stat[11] += m;
         }
     }
     __syncthreads();
@@ -674,19 +799,15 @@ __device__ bool rb_sort_particles(const RbArgs &a, uint32_t slot, RbShared &sh, 
 }
 
 // ------------------------------------------------------------------ the persistent loop
-__global__ void __launch_bounds__(kRB, 2) k_rebind_loop(RbArgs a) {
-    __shared__ __align__(16) unsigned char buf[kFront * (3 * 4 + 2)];
-    __shared__ uint32_t warp_tot[kRB / 32];
+__global__ void __launch_bounds__(kRB, 1) k_rebind_loop(RbArgs a) {
+    extern __shared__ __align__(16) unsigned char rb_dyn[];
+    __shared__ uint32_t warp_tot[kRbWarps];
     __shared__ uint32_t u[16];
-    __shared__ double st[8], tabM[32], tabY[32];
-    __shared__ float tabF[32];
+    __shared__ double st[8], tabM[32], tabY[32], sd[8];
+    __shared__ float tabF[32], sf[16];
     __shared__ uint32_t s_item;
-    RbShared sh{buf, warp_tot, u, st, tabM, tabY, tabF};
+    RbShared sh{rb_dyn, warp_tot, u, st, tabM, tabY, tabF, sf, sd};
     const int tid = threadIdx.x;
-    static_assert(kTile * (64 + 52 + 4 + 1) <= kFront * 14, "acceptance tile");
-    static_assert(7 * kKinTile * 8 <= kFront * 14, "sum tile");
-    static_assert(kSmallSort * 14 <= kFront * 14, "small sort");
-    static_assert((256 + 256 * (kRB / 32) + 1) * 4 <= kFront * 14, "radix counters");
     for (uint32_t guard = 0; guard <= a.n; ++guard) {
         if (tid == 0) s_item = atomicAdd(a.head, 1u);
         __syncthreads();
@@ -709,7 +830,7 @@ __global__ void __launch_bounds__(kRB, 2) k_rebind_loop(RbArgs a) {
         }
         __syncthreads();
         const uint32_t myrank = a.rank_of[slot];
-        unsigned long long *stat = a.stats ? a.stats + 8 * (size_t)slot : nullptr;
+        unsigned long long *stat = a.stats ? a.stats + kRbStats * (size_t)slot : nullptr;
         bool suspend = false;
         if (a.needsort[slot]) suspend = !rb_sort_particles(a, slot, sh, stat);
         for (uint32_t call = 0; !suspend; ++call) {
