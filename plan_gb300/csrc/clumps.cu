@@ -940,7 +940,7 @@ __device__ __forceinline__ void split_f(double d, float &hi, float &lo) {
 // and the host falls back to it). A record carries kDeferSpec when the earlier clump had not
 // finished its calls when it was observed (its holding could still change in that pass);
 // without the bit the clump saw that pass's final holding.
-constexpr int kDeferSlots = 8;
+constexpr int kDeferSlots = 16;
 constexpr uint32_t kDeferSpec = 0x80000000u;
 
 __device__ void defer_add(uint32_t *dset, uint8_t *dover, uint32_t *dmax, uint32_t slot, uint32_t ow, bool spec = true) {
@@ -2644,11 +2644,14 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
             std::vector<uint32_t> rerun;
             std::vector<uint8_t> rr(nlive + 1, 0);
             uint32_t low = kNone;  // lowest rank rerun or changed so far
+            uint64_t why_inv = 0, why_dov = 0, why_rerun = 0, why_changed = 0;
             for (uint32_t r = 0; r < nlive; ++r) {
                 const uint32_t sl = live[r];
                 bool again = inv[sl] != 0;
+                why_inv += again;
                 if (!again && dov[sl]) {
                     again = low != kNone && dm[sl] && dm[sl] - 1 >= low;
+                    why_dov += again;
                 } else if (!again) {
                     for (int j = 0; j < kDeferSlots && !again; ++j) {
                         const uint32_t d0 = ds[(size_t)sl * kDeferSlots + j];
@@ -2658,6 +2661,8 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                         const uint32_t d = d0 & ~kDeferSpec;
                         const bool spec = use_rounds || (d0 & kDeferSpec) != 0;
                         again = d < nlive && (rr[d] || (spec && changed[d]));
+                        why_rerun += again && rr[d];
+                        why_changed += again && !rr[d];
                     }
                 }
                 if (again) { rerun.push_back(sl); rr[r] = 1; }
@@ -2697,6 +2702,8 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                 for (uint32_t sl : rerun) pred_hash[sl] = hnow[sl];
             }
             trace.mark("rerun closure (invalid+deferred, changed)", rerun.size(), std::count(changed.begin(), changed.end(), 1));
+            trace.mark("  rerun reasons (lost a particle, overflowed record, partner reruns, partner changed)", why_inv, why_dov, why_rerun,
+                       why_changed);
 
             // blockers of each rerun clump: the rerun clumps of lower rank it met (skipped a
             // particle of, lost one to, or had one taken by); when its record overflowed, every
