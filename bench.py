@@ -49,6 +49,17 @@ WORKLOAD_NAME = ("16.7M-particle snapshot (2^24, float32): 60% uniform, 25% in 4
 # density, HOP), per unit for the density kernel: read the query (12 B), write the
 # density (8 B), the K_d neighbour list the reference builds (4 * K_d), the radius (4 B)
 DENSITY_BYTES_PER_POINT = 12 + 8 + 4 * KNN + 4
+# the clump stage's model: 28 bytes per member and pass (the member index, its position and
+# mass read once, its distance written); the rebinding launches count the members of the
+# clumps each one ran
+REBIND_BYTES_PER_MEMBER = 28
+# dram bytes read + written per unit, measured with ncu on smaller snapshots of the same
+# mixture (profiles/k_rebind_loop_workload2.md, profiles/k_density_f_workload2.md)
+REBIND_TRAFFIC_PER_MEMBER = 0.0
+DENSITY_TRAFFIC_PER_POINT = 0.0
+# the catalogue of the benchmarked snapshot as the unmodified reference writes it
+# (tests/golden/w2_16m, made by tests/golden/make_golden.py)
+GOLDEN_FULL = ROOT / "tests" / "golden" / "w2_16m" / "meta.json"
 
 
 def _peaks() -> tuple[float, str]:
@@ -110,13 +121,33 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def synth_lib() -> C.CDLL:
+    """The snapshot generator alone (plan_gb300/lib/libplan_synth.so, no CUDA), so that the CPU
+    arm never loads the GPU library."""
+    import plan_gb300 as pg  # structure layouts only; the GPU library is not loaded
+
+    path = ROOT / "plan_gb300" / "lib" / "libplan_synth.so"
+    if not path.exists():
+        from plan_gb300 import build as b
+
+        b.build()
+    L = C.CDLL(str(path))
+    L.plan_synth_default_spec.restype = C.c_int32
+    L.plan_synth_default_spec.argtypes = [C.c_int32, C.c_uint64, C.c_uint64, C.POINTER(pg.SynthSpec)]
+    L.plan_synth_records.restype = C.c_int32
+    L.plan_synth_records.argtypes = [C.POINTER(pg.SynthSpec), C.c_void_p, C.POINTER(pg.SynthInfo)]
+    L.plan_synth_four_pi_G_for_mean.restype = C.c_double
+    L.plan_synth_four_pi_G_for_mean.argtypes = [C.POINTER(pg.SynthSpec), C.c_int32, C.c_int32]
+    return L
+
+
 def make_records(n: int, seed: int, pinned: bool):
-    """The workload's .lis records in (page-locked) host memory; returns (tensor, spec, 4piG)."""
+    """The workload's .lis records in (page-locked) host memory; returns (tensor, 4piG)."""
     import torch
 
     import plan_gb300 as pg
 
-    L = pg.lib()
+    L = synth_lib()
     spec = pg.SynthSpec()
     rc = L.plan_synth_default_spec(WORKLOAD, n, seed, C.byref(spec))
     assert rc == 0
@@ -186,27 +217,64 @@ def cpu_sample(n: int, seed: int, threads: int, reps: int = 1, warmup: int = 0) 
 
 
 def run_reference(args) -> None:
-    """The reference arm: the CPU implementation of the path on the host cores."""
+    """The reference arm: the CPU implementation of the path on the host cores, on the GPU arm's
+    own snapshot (same size, seed and parameters). The snapshot is generated and written once,
+    untimed; every timed pass reads it and runs the whole path to the catalogue. The CPU code
+    keeps no state between passes, so no warm-up pass is run; passes continue until `steps` are
+    done or `--ref-budget` seconds have been spent (at least one pass), and the line reports
+    how many ran."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     from plan_gb300 import build as b
 
     b.build_oracle()
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+
     threads = os.cpu_count() or 1
-    n = args.sample_n
-    r = cpu_sample(n, SEED, threads, reps=args.steps, warmup=args.warmup)
-    per = [n / t for t in r["seconds"]]
-    value = args.steps * n / sum(r["seconds"])
-    sample = f"{n} particles of the same workload (same mixture and clump mass function, clump count scaled), {args.steps} snapshots"
+    n = args.n
+    times = []
+    with tempfile.TemporaryDirectory() as d:
+        d = Path(d)
+        rec, fourpig = make_records(n, SEED, pinned=False)
+        write_lis(d / "Snap.0000.ds.lis", rec.numpy(), n)
+        write_params(d / "para.txt", fourpig, threads)
+        del rec
+        while len(times) < args.steps and (not times or sum(times) + times[-1] <= args.ref_budget):
+            t0 = time.perf_counter()
+            o = oracle.Oracle(str(d / "Snap.0000.ds.lis"), str(d / "para.txt"), threads=threads, pow_mode=0)
+            o.find()
+            times.append(time.perf_counter() - t0)
+            o.close()
+            print(f"bench --impl reference: pass {len(times)} {times[-1]:.1f} s", file=sys.stderr, flush=True)
+    value = n * len(times) / sum(times)
+    sample = (f"the full {n}-particle snapshot of the GPU arm (seed {SEED}), read and processed to the catalogue in each of "
+              f"{len(times)} passes ({args.steps} requested; passes stop after {args.ref_budget:.0f} s)")
     line = {"impl": "reference", "metric": "particles/s", "value": value, "unit": "particles/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(r["seconds"]) / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD_NAME, "n_particles": N_FULL, "sample_particles": n, "knn": KNN, "hop": HOP, "nx": NX},
+            "steps": len(times), "requested_steps": args.steps, "warmup": 0, "requested_warmup": args.warmup,
+            "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD_NAME, "n_particles": n, "seed": SEED, "knn": KNN, "hop": HOP, "nx": NX},
             "cpu_baseline": {"value": value, "unit": "particles/s", "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "particles/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "per_step_particles_per_s": per}
+            "per_step_s": times}
     print(json.dumps(line), flush=True)
+
+
+def check_parity(cat, n: int, seed: int):
+    """The catalogue against the reference's for the benchmarked snapshot: the summary line and
+    the SHA-256 of peaks_at_*.txt must be equal. None for snapshots without a recorded one."""
+    import hashlib
+
+    if n != N_FULL or seed != SEED or not GOLDEN_FULL.exists():
+        return None
+    g = json.loads(GOLDEN_FULL.read_text())
+    with tempfile.TemporaryDirectory() as d:
+        cat.write_peaks(str(Path(d) / "res.txt"))
+        got = hashlib.sha256((Path(d) / g["peaks_file"]).read_bytes()).hexdigest()
+    return {"identical": got == g["peaks_sha256"] and cat.summary().strip() == g["summary"], "peaks_sha256": got,
+            "against": "catalogue of the unmodified reference on the same snapshot"}
 
 
 # ---------------------------------------------------------------- replicas
@@ -262,6 +330,8 @@ def run_gpu(args) -> None:
     v_host = lis_view(pg, rec_h.data_ptr(), n)
     L = pg.lib()
 
+    last = {}
+
     def step(view):
         h = C.c_void_p()
         rc = L.plan_find_clumps(f._h, C.byref(view), C.byref(p), 1, C.c_void_p(sp), C.byref(h))
@@ -269,7 +339,9 @@ def run_gpu(args) -> None:
             raise pg.PlanError(rc, f.error())
         cat = pg.Catalogue(h)
         nc = len(cat)
-        cat.close()
+        if "cat" in last:
+            last["cat"].close()
+        last["cat"] = cat  # the last catalogue is checked after the timed region
         return nc
 
     def barrier():
@@ -307,20 +379,34 @@ def run_gpu(args) -> None:
     cnt = f.counters()
     nclumps = int(cnt[7])
     tree_points = int(cnt[2])
+    rb_ms, rb_members = stage[19], int(cnt[24])  # the rebinding launches of the last timed step
+    parity = check_parity(last["cat"], n, replica_seed(rank))
     # end to end through the same call with host records (buffers and arenas are already sized
     # by the warm-up, so no separate warm-up of this leg)
-    total_e2e, per_e2e, _, _, _ = timed(v_host, args.steps)
+    e2e_steps = max(1, min(args.steps, args.e2e_steps))
+    total_e2e, per_e2e, _, _, _ = timed(v_host, e2e_steps)
+    last["cat"].close()
     h2d = int(f.counters()[20])
     d2h = int(f.counters()[21])
     value = aggregate(world, n, args.steps, total)
-    e2e_value = aggregate(world, n, args.steps, total_e2e)
+    e2e_value = aggregate(world, n, e2e_steps, total_e2e)
     peak, peak_kind = _peaks()
+    # the dominant kernel: the rebinding loop (one launch per pass; its time summed over the
+    # launches of a snapshot, CUDA events on the stream it runs on)
+    rb_bytes = REBIND_BYTES_PER_MEMBER * rb_members
+    rb_achieved = rb_bytes / (rb_ms / 1e3) / 1e9 if rb_ms > 0 else None
+    roof = {"kernel": "k_rebind_loop (Hill-sphere rebinding, every clump's calls on the device; all launches of one snapshot)",
+            "bound": "hbm", "achieved": rb_achieved, "peak": peak, "unit": "GB/s", "frac": rb_achieved / peak if rb_achieved else None,
+            "peak_kind": f"{peak_kind} HBM copy bandwidth", "traffic": REBIND_TRAFFIC_PER_MEMBER * rb_members,
+            "traffic_note": "dram bytes read+written per member from one ncu capture (profiles/), times the members of the step's launches",
+            "bytes_per_unit": REBIND_BYTES_PER_MEMBER, "units": rb_members, "kernel_ms": rb_ms,
+            "limited_by": "dependent FP64 update chains and exact ordered member sums, not bandwidth"}
     dens_avg = float(np.mean(dens_ms))
     achieved = DENSITY_BYTES_PER_POINT * tree_points / (dens_avg / 1e3) / 1e9 if dens_avg > 0 else None
-    roof = {"kernel": "k_density_f (KNN + median density, FP32-filtered exact traversal)", "bound": "hbm", "achieved": achieved,
-            "peak": peak, "unit": "GB/s", "frac": achieved / peak if achieved else None, "peak_kind": f"{peak_kind} HBM copy bandwidth",
-            "traffic": None, "bytes_per_unit": DENSITY_BYTES_PER_POINT, "units_per_launch": tree_points,
-            "launch_ms": dens_avg}
+    roof_dens = {"kernel": "k_density_f (KNN + median density, FP32-filtered exact traversal)", "bound": "hbm", "achieved": achieved,
+                 "peak": peak, "unit": "GB/s", "frac": achieved / peak if achieved else None, "peak_kind": f"{peak_kind} HBM copy bandwidth",
+                 "traffic": DENSITY_TRAFFIC_PER_POINT * tree_points, "bytes_per_unit": DENSITY_BYTES_PER_POINT,
+                 "units_per_launch": tree_points, "launch_ms": dens_avg}
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -336,13 +422,16 @@ def run_gpu(args) -> None:
                            "tree_points": tree_points, "clumps_found": nclumps, "parallelism": f"replicas{world}",
                            "l2": "inputs larger than L2 (records 738 MB, tree arrays several GB), no flush"},
                 "e2e": {"value": e2e_value, "unit": "particles/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                        "ms_per_step": total_e2e / args.steps},
-                "roofline": roof, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
+                        "ms_per_step": total_e2e / e2e_steps, "steps": e2e_steps},
+                "parity": parity,
+                "roofline": roof, "roofline_density": roof_dens, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
                 "snapshots_per_s": world * args.steps / (total / 1e3),
                 "latency_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99))},
                 "stage_ms": {"ingest_ghosts_keys": stage[0], "sort": stage[1], "sinks_tree": stage[2], "tree_tail": stage[3],
                              "density": stage[4], "densest": stage[5], "hop": stage[6], "clump_stage": stage[7],
-                             "catalogue": stage[8], "density_kernel": stage[20], "densest_kernel": stage[21]}}
+                             "catalogue": stage[8], "density_kernel": stage[20], "densest_kernel": stage[21],
+                             "rebinding": stage[12], "rebinding_kernel": stage[19]},
+                "rebinding": {"passes": int(cnt[12]), "launches": int(stage[14]), "reruns": int(cnt[14])}}
         print(json.dumps(line), flush=True)
     f.close()
     if dist is not None:
@@ -506,7 +595,9 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--n", type=int, default=N_FULL, help="particles per snapshot (default: the full workload)")
-    ap.add_argument("--sample-n", type=int, default=1 << 22, help="particles of the CPU sample snapshot")
+    ap.add_argument("--sample-n", type=int, default=1 << 22, help="particles of the CPU sample snapshot (GPU arm's cpu_baseline)")
+    ap.add_argument("--ref-budget", type=float, default=480.0, help="reference arm: seconds of timed full-size passes (at least one)")
+    ap.add_argument("--e2e-steps", type=int, default=3, help="steps of the end-to-end leg (at most --steps)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--serve", type=int, default=0, help="instead: K requests through the serving loop (plan_submit/plan_poll)")
     ap.add_argument("--serve-workers", type=int, default=3)

@@ -1,8 +1,9 @@
 """Build recipe for the in-tree native code.
 
 Compiles the CUDA translation units for sm_103a only and the host C++ with g++, links
-``plan_gb300/lib/libplan_gpu.so`` (the C ABI of ``include/plan_gpu.h``) and the drop-in
-command-line program ``plan_gb300/lib/plan_gpu``. All floating-point code is built without
+``plan_gb300/lib/libplan_gpu.so`` (the C ABI of ``include/plan_gpu.h``), the drop-in
+command-line program ``plan_gb300/lib/plan_gpu`` and ``plan_gb300/lib/libplan_synth.so`` (the
+snapshot generator of ``include/plan_synth.h`` alone, for callers without a GPU). All floating-point code is built without
 contraction (``--fmad=false`` / ``-ffp-contract=off``) so results round exactly like the
 reference's x86-64 build on both x86-64 and aarch64 hosts. Objects go to
 ``plan_gb300/_build/``; nothing is installed outside the tree.
@@ -83,6 +84,11 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
     if not _newer(lib, objs):
         _run(["g++", "-shared", "-o", str(lib), *map(str, objs), "-L" + str(cuda / "lib64"), "-lcudart", "-fopenmp",
               "-Wl,-rpath," + str(cuda / "lib64")])
+    # the snapshot generator alone (no CUDA): what the CPU-only benchmark arm loads
+    synth = OUT / "libplan_synth.so"
+    synth_o = OBJ / "synth.o"
+    if not _newer(synth, [synth_o]):
+        _run(["g++", "-shared", "-o", str(synth), str(synth_o), "-fopenmp"])
     cli = OUT / "plan_gpu"
     cli_src = CSRC / "host" / "cli.cpp"
     if not _newer(cli, [cli_src, lib] + headers):

@@ -2346,6 +2346,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
             rb_grid = std::max(1, nsm * std::max(1, per));
         }
         uint64_t loop_launches = 0, suspensions = 0;
+        c.counters[24] = 0;  // members of the clumps the rebinding launches ran (per launch, summed)
         // One pass of the device loop over `list` (key-rank order). Clumps that found the
         // member pool full stop with a consistent state; the pool is compacted and they
         // continue in another launch.
@@ -2409,15 +2410,28 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                 ra.err = c.d_err;
                 const unsigned grid = (unsigned)std::min<size_t>(todo.size(), (size_t)rb_grid);
                 double t_a = wall_ms();
+                if (c.kev[0]) cudaEventRecord(c.kev[0], s);
                 k_rebind_loop<<<grid, kRB, kRbSmem, s>>>(ra);
                 c.launches++;
                 ++loop_launches;
                 PLAN_CUDA(cudaGetLastError());
+                if (c.kev[1]) cudaEventRecord(c.kev[1], s);
                 std::vector<uint8_t> sus;
+                std::vector<uint32_t> mn_after;
                 r = st.down(sus, d_susp, nb);
+                if (!r) r = st.down(mn_after, ct.mn, C);
                 S.used = mark;
                 if (r) return r;
                 c.stage_ms[16] += wall_ms() - t_a;
+                float kms = 0.f;
+                if (c.kev[0] && c.kev[1] && cudaEventElapsedTime(&kms, c.kev[0], c.kev[1]) == cudaSuccess) c.stage_ms[19] += kms;
+                // the launch's work in the algorithmic model: the members of the clumps it ran
+                uint64_t launch_members = 0;
+                for (uint32_t sl : todo) launch_members += mn_after[sl];
+                c.counters[24] += launch_members;
+                if (trace.on)
+                    std::fprintf(stderr, "[plan]   rebinding launch: %zu clumps, %llu members, %.3f ms\n", todo.size(),
+                                 (unsigned long long)launch_members, (double)kms);
                 std::vector<uint32_t> next;
                 for (uint32_t sl : todo)
                     if (sus[sl]) next.push_back(sl);

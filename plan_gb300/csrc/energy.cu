@@ -51,8 +51,9 @@ __global__ void __launch_bounds__(256) k_group_kinetic(const float4 *pm, const f
         __syncthreads();
     }
     const double M = s[0][0];
-    const double xc = s[0][1] / M, yc = s[0][2] / M, zc = s[0][3] / M;
-    const double vx = s[0][4] / M, vy = s[0][5] / M, vz = s[0][6] / M;
+    // an empty (or massless) group has no centre: zeros, and no kinetic energy below
+    const double xc = M > 0.0 ? s[0][1] / M : 0.0, yc = M > 0.0 ? s[0][2] / M : 0.0, zc = M > 0.0 ? s[0][3] / M : 0.0;
+    const double vx = M > 0.0 ? s[0][4] / M : 0.0, vy = M > 0.0 ? s[0][5] / M : 0.0, vz = M > 0.0 ? s[0][6] / M : 0.0;
     __syncthreads();
     double ek = 0;
     for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) {

@@ -51,6 +51,7 @@ class ServeQueue {
         if (workers < 1) workers = 1;
         held_.assign(workers, 0);
         busy_.assign(workers, 0);
+        release_pending_.assign(workers, 0);
         assigned_.assign(workers, nullptr);
         for (int w = 0; w < workers; ++w) threads_.emplace_back([this, w] { worker_loop(w); });
     }
@@ -121,6 +122,11 @@ class ServeQueue {
         return releases_;
     }
     int workers() const { return (int)held_.size(); }
+    // once true, stays true: submit refuses everything from then on
+    bool stopping() const {
+        std::unique_lock<std::mutex> lk(mu_);
+        return stop_;
+    }
 
    private:
     // Start what can start; called with the lock held. Nothing starts once shutting down (a
@@ -151,9 +157,11 @@ class ServeQueue {
                     for (int w = 0; w < (int)held_.size(); ++w)
                         if (!busy_[w] && w != best) idle_other += held_[w];
                     if (held - idle_other + grow <= budget_ && idle_other > 0) {
+                        // the idle workers give their buffers back on their own threads, outside
+                        // the lock; the request started below waits until they have
                         for (int w = 0; w < (int)held_.size(); ++w)
                             if (!busy_[w] && w != best && held_[w]) {
-                                if (release_) release_(w);
+                                if (release_) release_pending_[w] = 1;
                                 held_[w] = 0;
                                 ++releases_;
                             }
@@ -182,13 +190,29 @@ class ServeQueue {
         }
     }
 
+    bool releases_pending_locked() const {
+        for (uint8_t f : release_pending_)
+            if (f) return true;
+        return false;
+    }
+
     void worker_loop(int w) {
         const int init_rc = init_ ? init_(w) : 0;
         std::unique_lock<std::mutex> lk(mu_);
         while (true) {
-            cv_work_.wait(lk, [&] { return stop_ || assigned_[w] != nullptr; });
+            cv_work_.wait(lk, [&] { return stop_ || assigned_[w] != nullptr || release_pending_[w]; });
+            if (release_pending_[w]) {  // give the buffers back without holding the lock
+                lk.unlock();
+                release_(w);
+                lk.lock();
+                release_pending_[w] = 0;
+                cv_done_.notify_all();
+                continue;
+            }
             if (assigned_[w] == nullptr) break;  // stopping, nothing assigned
             std::shared_ptr<ServeRequest> r = assigned_[w];
+            // the room this request was admitted into must be free before it allocates
+            cv_done_.wait(lk, [&] { return !releases_pending_locked(); });
             lk.unlock();
             r->t_start = std::chrono::steady_clock::now();
             const int rc = init_rc ? init_rc : run_(w, *r);
@@ -209,7 +233,7 @@ class ServeQueue {
     std::deque<std::shared_ptr<ServeRequest>> queue_;
     std::map<uint64_t, std::shared_ptr<ServeRequest>> all_;
     std::vector<uint64_t> held_;
-    std::vector<uint8_t> busy_;
+    std::vector<uint8_t> busy_, release_pending_;
     std::vector<std::shared_ptr<ServeRequest>> assigned_;
     std::vector<std::thread> threads_;
     uint64_t budget_, next_id_ = 0, peak_held_ = 0, releases_ = 0, started_ = 0;

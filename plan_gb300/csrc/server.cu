@@ -103,7 +103,12 @@ int plan_submit(plan_server *srv, const plan_lis_view *snap, const plan_params *
     const uint64_t id = srv->q->submit(plan_footprint_bytes(n, p), j);
     if (id == 0) {
         delete j;
+        const bool closing = srv->q->stopping();
         std::lock_guard<std::mutex> lk(srv->mu);
+        if (closing) {
+            srv->error = "the serving loop is shutting down and takes no more requests";
+            return plan::kErrArgument;
+        }
         srv->error = "the snapshot alone needs more device memory than the serving budget";
         return plan::kErrOutOfMemory;
     }

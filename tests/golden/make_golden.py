@@ -12,7 +12,9 @@ ref`) with its stage dump switched on, and stores under tests/golden/<case>/:
   (the per-clump member lists of --Save_Clumps are pinned by their SHA-256 in meta.json)
 
 Run it in a checkout where the reference is present:  python tests/golden/make_golden.py
-It needs the reference binary and the library's generator; nothing at test time runs it.
+(`python tests/golden/make_golden.py full_workload` writes tests/golden/w2_16m, the catalogue
+of the benchmarked 16.7M-particle snapshot). It needs the reference binary and the library's
+generator; nothing at test time runs it.
 """
 from __future__ import annotations
 
@@ -221,10 +223,50 @@ def dvs_variants() -> None:
             print(f"{name}: {files} {summary}")
 
 
+def full_workload() -> None:
+    """The benchmarked snapshot itself (bench.py's default: 16,777,216 particles of the
+    workload-2 mixture, seed 1), run by the reference without stage dumps, which would be
+    gigabytes at this size: its catalogue, its basic-results file and the catalogue's SHA-256,
+    which bench.py and the full-size GPU test compare with."""
+    import hashlib
+
+    import bench
+
+    with tempfile.TemporaryDirectory() as tmp:
+        tmp = Path(tmp)
+        (tmp / "in").mkdir()
+        rec, fourpig = bench.make_records(bench.N_FULL, bench.SEED, pinned=False)
+        lis = tmp / "in" / "Snap.0000.ds.lis"
+        bench.write_lis(lis, rec.numpy(), bench.N_FULL)
+        del rec
+        bench.write_params(tmp / "in" / "para.txt", fourpig, os.cpu_count() or 1)
+        out = tmp / "ref"
+        out.mkdir()
+        args = ["-c", "1", "-i", str(tmp / "in"), "-b", "Snap", "-p", "ds", "-f", "0:0", "-o", str(out / "res.txt"), "-t",
+                str(tmp / "in" / "para.txt"), "--Combined"]
+        r = subprocess.run([str(REF)] + args, cwd=out, capture_output=True, text=True, check=True)
+        summary = [ln for ln in r.stdout.splitlines() if "Finish clump finding" in ln]
+        assert len(summary) == 1, r.stdout
+        g = HERE / "w2_16m"
+        if g.exists():
+            shutil.rmtree(g)
+        g.mkdir()
+        pk = cases.find_peaks_file(out)
+        shutil.copy(pk, g / pk.name)
+        shutil.copy(out / "res_planetesimals.txt", g / "planetesimals.txt")
+        meta = {"case": "w2_16m", "n": bench.N_FULL, "seed": bench.SEED, "workload": bench.WORKLOAD,
+                "lis_sha256": hashlib.sha256(lis.read_bytes()).hexdigest(), "four_pi_G": fourpig, "summary": summary[0].strip(),
+                "peaks_file": pk.name, "peaks_sha256": hashlib.sha256(pk.read_bytes()).hexdigest()}
+        (g / "meta.json").write_text(json.dumps(meta, indent=1) + "\n")
+        print("w2_16m:", meta["summary"])
+
+
 def main() -> None:
     if not REF.exists():
         sys.exit(f"{REF} missing: run `make -C oracle ref` in a checkout with the reference")
     only = set(sys.argv[1:])
+    if "full_workload" in only:  # the benchmarked snapshot only on request: minutes of CPU time
+        full_workload()
     if not only or "multi_snapshot" in only:
         multi_snapshot()
     if not only or "variants" in only:

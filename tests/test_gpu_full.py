@@ -1,0 +1,59 @@
+"""The benchmarked snapshot itself on the GPU (needs a GB300).
+
+bench.py times 16,777,216 particles of the workload-2 mixture (seed 1). This test runs that
+snapshot once through plan_find_clumps, from device-resident records as the benchmark's
+timed steps do, and requires the catalogue the unmodified reference wrote for it
+(tests/golden/w2_16m): the same summary line and a byte-identical peaks_at_*.txt. At this
+size the clump stage meets its hardest cases: dozens of dependency levels between clumps in
+the Hill-sphere rebinding, clumps of several hundred thousand members and hundreds of calls.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import hashlib
+import json
+import os
+
+import pytest
+
+from conftest import GOLDEN, ROOT
+
+pytestmark = pytest.mark.gpu
+
+
+def test_benchmarked_snapshot_matches_reference(built, tmp_path):
+    import sys
+
+    import torch
+
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    g = json.loads((GOLDEN / "w2_16m" / "meta.json").read_text())
+    pg = built
+    rec_h, fourpig = bench.make_records(bench.N_FULL, bench.SEED, pinned=False)
+    assert fourpig == g["four_pi_G"]
+    rec_d = rec_h.to("cuda:0")
+    del rec_h
+    par = tmp_path / "para.txt"
+    bench.write_params(par, fourpig, os.cpu_count() or 1)
+    p = pg.params(str(par))
+    f = pg.Finder(0)
+    try:
+        v = bench.lis_view(pg, rec_d.data_ptr(), bench.N_FULL)
+        h = C.c_void_p()
+        rc = pg.lib().plan_find_clumps(f._h, C.byref(v), C.byref(p), 1, None, C.byref(h))
+        assert rc == 0, f.error()
+        cat = pg.Catalogue(h)
+        try:
+            assert cat.summary().strip() == g["summary"]
+            cat.write_peaks(str(tmp_path / "res.txt"))
+            got = (tmp_path / g["peaks_file"]).read_bytes()
+            assert hashlib.sha256(got).hexdigest() == g["peaks_sha256"]
+            assert got == (GOLDEN / "w2_16m" / g["peaks_file"]).read_bytes()
+        finally:
+            cat.close()
+    finally:
+        f.close()
+        del rec_d
+        torch.cuda.empty_cache()

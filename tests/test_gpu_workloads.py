@@ -120,14 +120,19 @@ def test_group_energies_against_fp64(request, built):
     vel = np.concatenate([q[1] for q in parts])
     mass = np.concatenate([q[2] for q in parts])
     off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64)
+    # an empty group after the first one: no energy, and the others unchanged
+    off_e = np.concatenate([off[:2], off[1:2], off[2:]]).astype(np.uint64)
     p = pg.params()
     pg.lib().plan_params_derive(__import__("ctypes").byref(p))
     f = pg.Finder(0)
     try:
         ek, ep, zeros = f.group_energies(pos, vel, mass, off, p)
+        ek_e, ep_e, zeros_e = f.group_energies(pos, vel, mass, off_e, p)
     finally:
         f.close()
-    assert zeros == 0
+    assert zeros == 0 and zeros_e == 0
+    assert ek_e[1] == 0.0 and ep_e[1] == 0.0
+    assert np.allclose(np.delete(ek_e, 1), ek, rtol=1e-12, atol=0) and np.allclose(np.delete(ep_e, 1), ep, rtol=1e-9, atol=0)
     G, s = p.grav_constant, p.q * p.Omega
     for g, (gp, gv, gm) in enumerate(parts):
         want_p = -G * fp64_potential_sum(gp, gm)
