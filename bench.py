@@ -50,13 +50,14 @@ WORKLOAD_NAME = ("16.7M-particle snapshot (2^24, float32): 60% uniform, 25% in 4
 # density (8 B), the K_d neighbour list the reference builds (4 * K_d), the radius (4 B)
 DENSITY_BYTES_PER_POINT = 12 + 8 + 4 * KNN + 4
 # the clump stage's model: 28 bytes per member and pass (the member index, its position and
-# mass read once, its distance written); the rebinding launches count the members of the
-# clumps each one ran
+# mass read once, its distance written); each rebinding pass counts the members of the
+# clumps it ran
 REBIND_BYTES_PER_MEMBER = 28
 # dram bytes read + written per unit, measured with ncu on smaller snapshots of the same
-# mixture (profiles/k_rebind_loop_workload2.md, profiles/k_density_f_workload2.md)
-REBIND_TRAFFIC_PER_MEMBER = 0.0
-DENSITY_TRAFFIC_PER_POINT = 0.0
+# mixture (profiles/k_rebind_loop_workload2.md, profiles/k_density_f_workload2.md); traffic grows with
+# the units processed, so a full-size launch's traffic is taken as units times these figures
+REBIND_TRAFFIC_PER_MEMBER = (167_780_608 + 45_761_280) / 260_562    # first launch, 1M snapshot: 819.5 B
+DENSITY_TRAFFIC_PER_POINT = (928_974_848 + 483_069_184) / 6_736_104  # 4M snapshot: 209.6 B
 # the catalogue of the benchmarked snapshot as the unmodified reference writes it
 # (tests/golden/w2_16m, made by tests/golden/make_golden.py)
 GOLDEN_FULL = ROOT / "tests" / "golden" / "w2_16m" / "meta.json"
@@ -398,7 +399,7 @@ def run_gpu(args) -> None:
     roof = {"kernel": "k_rebind_loop (Hill-sphere rebinding, every clump's calls on the device; all launches of one snapshot)",
             "bound": "hbm", "achieved": rb_achieved, "peak": peak, "unit": "GB/s", "frac": rb_achieved / peak if rb_achieved else None,
             "peak_kind": f"{peak_kind} HBM copy bandwidth", "traffic": REBIND_TRAFFIC_PER_MEMBER * rb_members,
-            "traffic_note": "dram bytes read+written per member from one ncu capture (profiles/), times the members of the step's launches",
+            "traffic_note": "dram bytes read+written per member from one ncu capture (profiles/), times the members of the step's passes",
             "bytes_per_unit": REBIND_BYTES_PER_MEMBER, "units": rb_members, "kernel_ms": rb_ms,
             "limited_by": "dependent FP64 update chains and exact ordered member sums, not bandwidth"}
     dens_avg = float(np.mean(dens_ms))

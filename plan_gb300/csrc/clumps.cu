@@ -2346,7 +2346,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
             rb_grid = std::max(1, nsm * std::max(1, per));
         }
         uint64_t loop_launches = 0, suspensions = 0;
-        c.counters[24] = 0;  // members of the clumps the rebinding launches ran (per launch, summed)
+        c.counters[24] = 0;  // members of the clumps each rebinding pass ran, summed over the passes
         // One pass of the device loop over `list` (key-rank order). Clumps that found the
         // member pool full stop with a consistent state; the pool is compacted and they
         // continue in another launch.
@@ -2425,10 +2425,8 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                 c.stage_ms[16] += wall_ms() - t_a;
                 float kms = 0.f;
                 if (c.kev[0] && c.kev[1] && cudaEventElapsedTime(&kms, c.kev[0], c.kev[1]) == cudaSuccess) c.stage_ms[19] += kms;
-                // the launch's work in the algorithmic model: the members of the clumps it ran
                 uint64_t launch_members = 0;
                 for (uint32_t sl : todo) launch_members += mn_after[sl];
-                c.counters[24] += launch_members;
                 if (trace.on)
                     std::fprintf(stderr, "[plan]   rebinding launch: %zu clumps, %llu members, %.3f ms\n", todo.size(),
                                  (unsigned long long)launch_members, (double)kms);
@@ -2443,6 +2441,12 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                 }
                 todo.swap(next);
             }
+            // the pass's work in the algorithmic model: the members of the clumps it ran, each
+            // once however many launches (after member-pool compactions) it took
+            std::vector<uint32_t> mn_end;
+            int r = st.down(mn_end, ct.mn, C);
+            if (r) return r;
+            for (uint32_t sl : list) c.counters[24] += mn_end[sl];
             return kOk;
         };
         // Rounds until no clump grows. Clumps in `waiting` start once every clump listed as
