@@ -56,7 +56,7 @@ int Context::ensure(Arena &a, size_t bytes) {
 // (T = 1.5625 n); the exact count is known, and the arena grown to it, during the build.
 static void footprint(uint64_t n, uint64_t &arena, uint64_t &scratch) {
     uint64_t T = n + n * 9 / 16 + 1024;
-    arena = T * kArenaBytesPerTreePoint + (64ull << 20);
+    arena = arena_bytes_for(T);
     scratch = (4 * n + 1024) * 40 > n * kScratchBytesPerParticle ? (4 * n + 1024) * 40 : n * kScratchBytesPerParticle;
     scratch += 64ull << 20;
 }

@@ -1935,7 +1935,15 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
     ct.sub_head = A.get<uint32_t>(C + 1); ct.sub_tail = A.get<uint32_t>(C + 1);
     Pool &P = st.P;
     const uint32_t m0 = hg.n_members;
-    P.cap = (uint32_t)std::min<uint64_t>(0xfffffff0ull, 6ull * m0 + Tu + 4096);
+    {
+        // the member pool: generous (40 x the HOP members + 6 x the tree points) where the
+        // arena has room, keeping ~256 B per tree point for what the clump stage allocates
+        // after it; never below the former 6 x members + tree points
+        const uint64_t want = 40ull * m0 + 6ull * Tu + 4096, floor_cap = 6ull * m0 + Tu + 4096;
+        const uint64_t used = (A.used + 255) & ~uint64_t(255), reserve = 256ull * Tu + (64ull << 20);
+        const uint64_t room = A.cap > used + reserve ? (A.cap - used - reserve) / 24 : 0;
+        P.cap = (uint32_t)std::min<uint64_t>(0xfffffff0ull, std::max(floor_cap, std::min(want, room)));
+    }
     P.idx = A.get<uint32_t>(P.cap);
     P.dist = A.get<double>(P.cap);
     st.alt_idx = A.get<uint32_t>(P.cap);
@@ -2947,6 +2955,8 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
     for (auto &e : ev) cudaEventDestroy(e);
     c.counters[7] = cat->clumps.size();
     c.counters[21] = d2h;
+    c.counters[25] = c.arena.peak;  // bytes of the snapshot arena used at most, and its size
+    c.counters[26] = c.arena.cap;
     if (out) *out = cat;
     else delete cat;
     return kOk;

@@ -763,7 +763,7 @@ int build_tree(Context &c, const plan_lis_view &v, plan_params &p, int first_fil
     if (Tmax >= 0xfffffff0ull) return kErrUnsupported;
     // phase B (snapshot arena): everything the later stages keep, sized by the exact count
     {
-        int erc = c.ensure(c.arena, (size_t)Tmax * kArenaBytesPerTreePoint + (64u << 20) + (selected ? (size_t)N * 4 : 0));
+        int erc = c.ensure(c.arena, (size_t)arena_bytes_for(Tmax) + (selected ? (size_t)N * 4 : 0));
         if (erc) return erc;
     }
     c.arena.used = 0;

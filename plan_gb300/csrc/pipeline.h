@@ -124,6 +124,17 @@ int launch_densest(Context &c, const plan_params &p, uint32_t k, double threshol
 // and the scratch bytes per input particle; used for sizing and for admission.
 constexpr uint64_t kArenaBytesPerTreePoint = 512;
 constexpr uint64_t kScratchBytesPerParticle = 160;
+// Room for the clump stage's member pool beyond that: a larger pool means fewer compactions
+// (and fewer relaunches) while the rebinding loop writes fresh segments. Capped so that the
+// largest snapshots still fit the device.
+constexpr uint64_t kPoolBytesPerTreePoint = 800;
+constexpr uint64_t kPoolBytesMax = 24ull << 30;
+
+// The snapshot arena for T tree points.
+inline uint64_t arena_bytes_for(uint64_t T) {
+    const uint64_t pool = T * kPoolBytesPerTreePoint < kPoolBytesMax ? T * kPoolBytesPerTreePoint : kPoolBytesMax;
+    return T * kArenaBytesPerTreePoint + pool + (64ull << 20);
+}
 
 inline unsigned grid_for(size_t n, int threads) {
     size_t b = (n + threads - 1) / threads;
