@@ -41,10 +41,13 @@ constexpr uint32_t kRbSmall = 4096;           // members sorted in shared memory
 constexpr uint32_t kWaitLimit = 1u << 25;     // bounded waits on blockers (about 30 s)
 constexpr uint32_t kCallLimit = 1u << 20;     // calls of one clump in one launch
 constexpr int kRbStats = 32;                  // counters per slot
-// dynamic shared memory: the largest phase is the frontier / the small sort
-constexpr size_t kRbSmem = 14 * (kRbFront > kRbSmall ? kRbFront : kRbSmall);
+// dynamic shared memory: the largest of the frontier, the small sort and the acceptance
+// tile (per candidate: FP64 position and velocity, index, FP32 form, taken flag)
+constexpr size_t kRbTileBytes = (size_t)kRB * (64 + 4 + sizeof(CandF) + 1);
+constexpr size_t kRbSmem14 = 14 * (kRbFront > kRbSmall ? kRbFront : kRbSmall);
+constexpr size_t kRbSmem = kRbSmem14 > kRbTileBytes ? kRbSmem14 : kRbTileBytes;
 static_assert(kRbFront * 14 <= kRbSmem, "frontier");
-static_assert((size_t)kRB * 68 <= kRbSmem, "acceptance tile");
+static_assert(kRbTileBytes <= kRbSmem, "acceptance tile");
 static_assert(kRbSmall * 14 <= kRbSmem, "small sort");
 static_assert((256 + 256 * kRbWarps + 1) * 4 <= kRbSmem, "radix counters");
 
@@ -276,10 +279,17 @@ __device__ uint32_t rb_call(const RbArgs &a, uint32_t slot, uint32_t myrank, RbS
     const uint32_t nel = s_nel;
     const long long t1 = clock64();
     // 4) the reference's sequential acceptance (src/tree.hpp:4686-4706), 512 candidates at a
-    // time. Every thread holds one candidate: q, its FP32 form in registers, its FP64
-    // position and velocity in shared memory.
+    // time. Every thread holds one candidate (its FP32 form in registers; the FP64 position
+    // and velocity, the index, the FP32 form and the taken flag also in shared memory). The
+    // block finds the first bound candidate; warp 0 takes it and then goes on alone through
+    // the next candidates, 32 at a time, as long as each 32 holds a bound one (no block
+    // barrier per acceptance where acceptances are dense); the block search resumes after a
+    // 32 without any.
     double4_32a *tpos = reinterpret_cast<double4_32a *>(sh.buf), *tvel = tpos + kRB;
     uint32_t *tq = reinterpret_cast<uint32_t *>(tvel + kRB);
+    CandF *tf = reinterpret_cast<CandF *>(tq + kRB);
+    uint8_t *ttk = reinterpret_cast<uint8_t *>(tf + kRB);
+    uint32_t &s_pos = sh.u[8];
     const float G32 = (float)a.cp.G, shear32 = (float)a.cp.shear;
     double comp = 0.0;      // warp 0, lane c < 6: component c of the state (x y z vx vy vz)
     double M = sh.st[0];    // warp 0: the mass
@@ -308,6 +318,91 @@ __device__ uint32_t rb_call(const RbArgs &a, uint32_t slot, uint32_t myrank, RbS
             sh.sd[6] = M;
         }
     }
+    // warp 0 takes candidate j of the tile: the reference's update (src/tree.hpp:4696-4701,
+    // the new mass multiplies the old centre), lane c < 6 updating component c as
+    // RN(RN(RN(c M') + RN(m q_c)) / M'); the new state is published in shared memory
+    auto take = [&](uint32_t j) {
+        const unsigned full = 0xffffffffu;
+        const long long tu0 = clock64();
+        const double m = tpos[j].w;
+        if (!(tab_i < tab_n && dbits(m) == dbits(tab_m))) {
+            // the next masses M_{l+1} = RN(M_l + m) on the grid of M's binade (exact while
+            // they stay inside it), and their correctly rounded reciprocals
+            tab_m = m;
+            tab_i = 0;
+            tab_n = 0;
+            const uint64_t mb = dbits(M);
+            const uint32_t ex = (uint32_t)(mb >> 52) & 0x7ffu;
+            long long dn = 0;
+            if ((mb >> 63) == 0 && ex > 60u && ex < 2000u && grid_term(m, ex, dn) && dn > 0) {
+                const long long n0 = (long long)((mb & 0xfffffffffffffull) | (1ull << 52));
+                const long long nl = n0 + (long long)(lane + 1) * dn;
+                const bool ok = nl > (1LL << 52) && nl <= (1LL << 53);
+                const unsigned okm = __ballot_sync(full, ok);
+                const unsigned edge = __ballot_sync(full, ok && nl == (1LL << 53));
+                int cnt = (~okm) ? __ffs(~okm) - 1 : 32;
+                if (edge) cnt = min(cnt, __ffs(edge));
+                if (lane < cnt) {
+                    const double Ml = grid_value(nl, ex);
+                    float fh, fl;
+                    split_any(Ml, fh, fl);
+                    sh.tabM[lane] = Ml;
+                    sh.tabY[lane] = __drcp_rn(Ml);
+                    sh.tabF[lane] = fh;
+                }
+                tab_n = cnt;
+                __syncwarp();
+            }
+        }
+        const long long tu1 = clock64();
+        double Mn, y;
+        float Mnf;
+        if (tab_i < tab_n) {
+            Mn = sh.tabM[tab_i];
+            y = sh.tabY[tab_i];
+            Mnf = sh.tabF[tab_i];
+            ++tab_i;
+        } else {
+            Mn = M + m;
+            y = __drcp_rn(Mn);
+            float fl;
+            split_any(Mn, Mnf, fl);
+            tab_n = 0;
+        }
+        if (lane < 6) {
+            // each lane loads its own component (one shared-memory load; a select over the
+            // whole position and velocity costs several hundred cycles here)
+            const double qc = reinterpret_cast<const double *>(lane < 3 ? &tpos[j] : &tvel[j])[lane < 3 ? lane : lane - 3];
+            const double num = comp * Mn + m * qc;
+            if ((dbits(num) << 1) == 0) {
+                comp = num;  // the quotient keeps the numerator's zero
+            } else {
+                const double q0 = num * y;
+                comp = fma(fma(-q0, Mn, num), y, q0);
+            }
+            float h, l;
+            if (stat && lane == 0) sh.u[15] += (uint32_t)(clock64() - tu1);
+            split_f(comp, h, l);  // the FP64 pipe is idle here: its conversions beat the integer split
+            sh.sf[lane] = h;
+            sh.sf[6 + lane] = l;
+            sh.sd[lane] = comp;
+        }
+        M = Mn;
+        if (lane == 0) {
+            sh.sf[12] = Mnf;
+            sh.sd[6] = Mn;
+            const uint32_t q2 = tq[j];
+            // the lowest rank keeps the particle; who lost one is found after the pass
+            atomicMin(&a.owner[q2], myrank);
+            elig[nacc] = q2;  // accepted ones overwrite candidates already consumed
+            if (stat) {
+                sh.u[13] += (uint32_t)(clock64() - tu0);
+                sh.u[14] += (uint32_t)(tu1 - tu0);
+            }
+        }
+        ++nacc;
+        __syncwarp();
+    };
     // the prefetched candidate of the next tile
     uint32_t nq = kNone, now_ = kNone, ntn = kNone;
     double4_32a np = make_double4_32a(0, 0, 0, 0), nv = make_double4_32a(0, 0, 0, 0);
@@ -323,6 +418,7 @@ __device__ uint32_t rb_call(const RbArgs &a, uint32_t slot, uint32_t myrank, RbS
     }
     for (uint32_t base = 0; base < nel; base += kRB) {
         const uint32_t q = nq;
+        const uint32_t tlen = min((uint32_t)kRB, nel - base);
         const bool valid = q != kNone;
         bool taken = true;
         CandF cf;
@@ -350,7 +446,9 @@ __device__ uint32_t rb_call(const RbArgs &a, uint32_t slot, uint32_t myrank, RbS
             split_any(nv.z, cf.vh[2], cf.vl[2]);
             float wl;
             split_any(np.w, cf.w, wl);
+            tf[tid] = cf;
         }
+        ttk[tid] = taken ? 1 : 0;
         nq = kNone;
         if (base + kRB + tid < nel) {  // prefetch (accepted ones are written below base + kRB only)
             nq = elig[base + kRB + tid];
@@ -390,89 +488,41 @@ __device__ uint32_t rb_call(const RbArgs &a, uint32_t slot, uint32_t myrank, RbS
             }
             if (f == kNone) break;  // the rest of the tile is not bound
             if (tid < 32) {
-                const long long tu0 = clock64();
                 const unsigned full = 0xffffffffu;
-                const double m = tpos[f].w;
-                if (!(tab_i < tab_n && dbits(m) == dbits(tab_m))) {
-                    // the next masses M_{l+1} = RN(M_l + m) on the grid of M's binade (exact
-                    // while they stay inside it), and their correctly rounded reciprocals
-                    tab_m = m;
-                    tab_i = 0;
-                    tab_n = 0;
-                    const uint64_t mb = dbits(M);
-                    const uint32_t ex = (uint32_t)(mb >> 52) & 0x7ffu;
-                    long long dn = 0;
-                    if ((mb >> 63) == 0 && ex > 60u && ex < 2000u && grid_term(m, ex, dn) && dn > 0) {
-                        const long long n0 = (long long)((mb & 0xfffffffffffffull) | (1ull << 52));
-                        const long long nl = n0 + (long long)(lane + 1) * dn;
-                        const bool ok = nl > (1LL << 52) && nl <= (1LL << 53);
-                        const unsigned okm = __ballot_sync(full, ok);
-                        const unsigned edge = __ballot_sync(full, ok && nl == (1LL << 53));
-                        int cnt = (~okm) ? __ffs(~okm) - 1 : 32;
-                        if (edge) cnt = min(cnt, __ffs(edge));
-                        if (lane < cnt) {
-                            const double Ml = grid_value(nl, ex);
-                            float fh, fl;
-                            split_any(Ml, fh, fl);
-                            sh.tabM[lane] = Ml;
-                            sh.tabY[lane] = __drcp_rn(Ml);
-                            sh.tabF[lane] = fh;
+                take(f);
+                // warp 0 alone through the next candidates while acceptances are dense
+                uint32_t at = f + 1;
+                while (at < tlen) {
+                    const uint32_t k = at + lane;
+                    bool bd = false, un = false;
+                    if (k < tlen && !ttk[k]) {
+                        float shv[6], slv[6];
+                        for (int c = 0; c < 6; ++c) {
+                            shv[c] = sh.sf[c];
+                            slv[c] = sh.sf[6 + c];
                         }
-                        tab_n = cnt;
-                        __syncwarp();
+                        const int r = bound_hilo_fast(tf[k], sh.sf[12], shv, slv, G32, shear32);
+                        if (r >= 0) bd = r == 1;
+                        else un = true;
                     }
-                }
-                const long long tu1 = clock64();
-                double Mn, y;
-                float Mnf;
-                if (tab_i < tab_n) {
-                    Mn = sh.tabM[tab_i];
-                    y = sh.tabY[tab_i];
-                    Mnf = sh.tabF[tab_i];
-                    ++tab_i;
-                } else {
-                    Mn = M + m;
-                    y = __drcp_rn(Mn);
-                    float fl;
-                    split_any(Mn, Mnf, fl);
-                    tab_n = 0;
-                }
-                // src/tree.hpp:4696-4701 (the new mass multiplies the old centre): lane c < 6
-                // updates component c as RN(RN(RN(c M') + RN(m q_c)) / M')
-                if (lane < 6) {
-                    const double4_32a p = tpos[f], v = tvel[f];
-                    const double qc = lane == 0 ? p.x : lane == 1 ? p.y : lane == 2 ? p.z : lane == 3 ? v.x : lane == 4 ? v.y : v.z;
-                    const double num = comp * Mn + m * qc;
-                    if ((dbits(num) << 1) == 0) {
-                        comp = num;  // the quotient keeps the numerator's zero
-                    } else {
-                        const double q0 = num * y;
-                        comp = fma(fma(-q0, Mn, num), y, q0);
+                    if (un) {
+                        bd = bound_fp64(tpos[k], tvel[k], sh.sd[6], sh.sd[0], sh.sd[1], sh.sd[2], sh.sd[3], sh.sd[4], sh.sd[5], a.cp);
+                        if (stat) atomicAdd(&sh.u[12], 1u);
                     }
-                    float h, l;
-                    if (stat && lane == 0) sh.u[15] += (uint32_t)(clock64() - tu1);
-                    split_any(comp, h, l);
-                    sh.sf[lane] = h;
-                    sh.sf[6 + lane] = l;
-                    sh.sd[lane] = comp;
-                }
-                M = Mn;
-                if (lane == 0) {
-                    sh.sf[12] = Mnf;
-                    sh.sd[6] = Mn;
-                    const uint32_t q2 = tq[f];
-                    // the lowest rank keeps the particle; who lost one is found after the pass
-                    atomicMin(&a.owner[q2], myrank);
-                    elig[nacc] = q2;  // accepted ones overwrite candidates already consumed
-                    if (stat) {
-                        sh.u[13] += (uint32_t)(clock64() - tu0);
-                        sh.u[14] += (uint32_t)(tu1 - tu0);
+                    const unsigned bb = __ballot_sync(full, bd);
+                    if (!bb) {  // none of these 32 is bound: leave them, back to the block search
+                        at = min(at + 32u, tlen);
+                        break;
                     }
+                    const uint32_t j = at + (uint32_t)(__ffs(bb) - 1);
+                    take(j);
+                    at = j + 1;
                 }
-                ++nacc;
+                if (lane == 0) s_pos = at;
             }
             __syncthreads();
-            pos = f + 1;
+            pos = s_pos;
+            if (pos >= tlen) break;
         }
         __syncthreads();
     }
