@@ -651,7 +651,7 @@ __device__ bool rb_sort_particles(const RbArgs &a, uint32_t slot, RbShared &sh, 
     if (wid < 7) {
         const long long ts = clock64();
         const double *tsrc = wid < 4 ? reinterpret_cast<const double *>(a.tm0) + wid : reinterpret_cast<const double *>(a.tm1) + (wid - 4);
-        constexpr int kK = 4;  // terms per lane and window
+        constexpr int kK = 2;  // terms per lane and window
         constexpr uint32_t kW = 32 * kK;
         uint32_t qa[kK], qb[kK];
         double x[kK], nx[kK];
