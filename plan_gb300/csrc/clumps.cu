@@ -511,29 +511,77 @@ __global__ void k_saddle_apply(uint32_t ns, const uint32_t *saddle_of, const dou
     code[saddle_of[q]] = (sdens[q] < limit) ? 0 : 1;
 }
 
-// Serial predator/prey resolution in key order (src/tree.hpp:3894-3951), one thread.
-__global__ void k_resolve(uint32_t C, CT ct, const uint32_t *cnt, const uint32_t *off, const uint8_t *code, const uint32_t *p2_of,
-                          uint32_t *pairs, uint32_t *npairs, uint32_t *del_keys, uint32_t *ndel, uint32_t *nunknown) {
-    if (threadIdx.x || blockIdx.x) return;
+// candidate -> its predator's slot
+__global__ void k_cand_owner(uint32_t C, const uint32_t *cnt, const uint32_t *off, uint32_t *cp1) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= C) return;
+    const uint32_t o = off[s], n = cnt[s];
+    for (uint32_t k = 0; k < n; ++k) cp1[o + k] = s;
+}
+
+// the candidates the resolution acts on: eat (code 1) or unknown key (code 4)
+__global__ void k_flag_resolve(uint32_t ncand, const uint8_t *code, uint32_t *flag) {
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= ncand) return;
+    flag[k] = (code[k] == 1 || code[k] == 4) ? 1u : 0u;
+}
+
+__global__ void k_scatter_flagged(uint32_t n, const uint32_t *flag, const uint32_t *pos, uint32_t *list) {
+    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n && flag[k]) list[pos[k]] = k;
+}
+
+// Serial predator/prey resolution in key order (src/tree.hpp:3894-3951) over the listed
+// candidates in candidate order (slots in key order, each slot's candidates in ball order);
+// the candidates left out (self, not bound, deep saddle) change nothing there. One warp:
+// the lanes fetch 32 candidates with what does not change during the walk (predator,
+// prey, code, whether the predator is alive, the prey's key), then the warp walks them in
+// order, reading and clearing the masks.
+__global__ void k_resolve(const uint32_t *list, const uint32_t *nlist, const uint32_t *cp1, CT ct, const uint8_t *code,
+                          const uint32_t *p2_of, uint32_t *pairs, uint32_t *npairs, uint32_t *del_keys, uint32_t *ndel, uint32_t *nunknown) {
+    const int lane = threadIdx.x;
+    if (blockIdx.x || lane >= 32) return;
+    const unsigned full = 0xffffffffu;
     uint32_t np = 0, nd = *ndel, nu = 0;
-    for (uint32_t p1 = 0; p1 < C; ++p1) {
-        if (!(ct.alive[p1] && ct.mask[p1])) continue;
-        for (uint32_t k = off[p1]; k < off[p1] + cnt[p1]; ++k) {
-            uint8_t cd = code[k];
-            if (cd == 3) continue;
-            if (cd == 4) { ++nu; continue; }
-            uint32_t p2 = p2_of[k];
-            if (!ct.mask[p2] || cd != 1) continue;
-            ct.mask[p2] = 0;
-            pairs[2 * np] = p1;
-            pairs[2 * np + 1] = p2;
+    const uint32_t n = *nlist;
+    for (uint32_t base = 0; base < n; base += 32) {
+        uint32_t p1 = 0, p2 = 0, key2 = 0, cd = 0, al = 0;
+        if (base + lane < n) {
+            const uint32_t k = list[base + lane];
+            p1 = cp1[k];
+            cd = code[k];
+            al = ct.alive[p1] ? 1u : 0u;
+            if (cd == 1) {
+                p2 = p2_of[k];
+                key2 = ct.key[p2];
+            }
+        }
+        const uint32_t cnt = min(32u, n - base);
+        for (uint32_t j = 0; j < cnt; ++j) {
+            const uint32_t q1 = __shfl_sync(full, p1, j), q2 = __shfl_sync(full, p2, j), kk = __shfl_sync(full, key2, j);
+            const uint32_t c = __shfl_sync(full, cd, j), a = __shfl_sync(full, al, j);
+            if (!(a && ct.mask[q1])) continue;
+            if (c == 4) {
+                ++nu;
+                continue;
+            }
+            if (!ct.mask[q2]) continue;
+            if (lane == 0) {
+                ct.mask[q2] = 0;
+                pairs[2 * np] = q1;
+                pairs[2 * np + 1] = q2;
+                del_keys[nd] = kk;
+            }
             ++np;
-            del_keys[nd++] = ct.key[p2];
+            ++nd;
+            __syncwarp();  // the cleared mask is seen by the whole warp from here on
         }
     }
-    *npairs = np;
-    *ndel = nd;
-    *nunknown += nu;
+    if (lane == 0) {
+        *npairs = np;
+        *ndel = nd;
+        *nunknown += nu;
+    }
 }
 
 // Waves of predators: a predator that eats an earlier predator waits for it.
@@ -1842,13 +1890,17 @@ static double wall_ms() {
 // PLAN_TRACE=1 in the environment prints the progress of FindPlanetesimals to stderr (the
 // stream is synchronised at every mark, so traced runs are slower; off by default).
 struct Trace {
-    bool on = false;
+    bool on = false, fine_on = false;  // PLAN_TRACE=1: stages; 2: also the steps inside a merge sweep
     cudaStream_t s = nullptr;
     double t0 = 0, last = 0;
     Trace(cudaStream_t st) : s(st) {
         const char *e = std::getenv("PLAN_TRACE");
         on = e && *e && *e != '0';
+        fine_on = on && *e == '2';
         t0 = last = wall_ms();
+    }
+    void fine(const char *what, long long a = -1, long long b = -1) {
+        if (fine_on) mark(what, a, b);
     }
     void mark(const char *what, long long a = -1, long long b = -1, long long c = -1, long long d = -1) {
         if (!on) return;
@@ -1869,6 +1921,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
     for (auto &e : ev) cudaEventCreate(&e);
     cudaEventRecord(ev[0], s);
     Trace trace(s);
+    c.counters[27] = 0;  // saddle queries of the merge sweeps left to the exact heap path (ties)
     const DevTree &tr = c.tree;
     const uint32_t Tu = tr.Tu, N = c.n_input;
     // kernel choice and thresholds (src/tree.hpp:3576-3660), host scalars
@@ -2025,6 +2078,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
         if (hill_mode) {
             rc = st.hill(live);
             if (rc) return rc;
+            trace.fine("  Hill radii (clumps)", (long long)live.size());
         }
         double max_radius = 0.;
         const uint32_t start_num = num_planetesimals;
@@ -2061,6 +2115,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                 if (rc) return rc;
             }
             KTree kct = ktree_of(ctree);
+            trace.fine("  clump tree (clumps)", nct);
             // candidates
             uint32_t ncand = 0;
             if (nct) {
@@ -2079,36 +2134,42 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
             uint8_t *d_code = A.get<uint8_t>(ncand + 1);
             double *d_sq = A.get<double>(3 * (size_t)ncand + 3), *d_sest = A.get<double>(ncand + 1), *d_sden = A.get<double>(ncand + 1);
             uint32_t *d_sof = A.get<uint32_t>(ncand + 1);
+            uint32_t *d_rfl = A.get<uint32_t>(ncand + 1), *d_rpos = A.get<uint32_t>(ncand + 1), *d_rlist = A.get<uint32_t>(ncand + 1);
+            uint32_t *d_nrl = st.d_u + 12;  // candidates the resolution acts on
             if (A.failed) return kErrOutOfMemory;
+            PLAN_CUDA(cudaMemsetAsync(d_nrl, 0, 4, s));
             uint32_t nsaddle = 0;
             if (ncand) {
                 k_ball_clumps<<<grid_for(C, 128), 128, 0, s>>>(1, C, ct, kct, hill_mode, hillf, max_radius, d_cnt, d_off, d_cand, c.d_err);
-                // candidate -> predator slot
-                std::vector<uint32_t> hcnt, hoff;
-                rc = st.down(hcnt, d_cnt, C);
-                if (!rc) rc = st.down(hoff, d_off, C);
-                if (rc) return rc;
-                std::vector<uint32_t> cp1(ncand);
-                for (uint32_t sl = 0; sl < C; ++sl)
-                    for (uint32_t k = 0; k < hcnt[sl]; ++k) cp1[hoff[sl] + k] = sl;
-                PLAN_CUDA(cudaMemcpyAsync(d_cp1, cp1.data(), (size_t)ncand * 4, cudaMemcpyHostToDevice, s));
+                k_cand_owner<<<grid_for(C, 256), 256, 0, s>>>(C, d_cnt, d_off, d_cp1);
                 PLAN_CUDA(cudaMemsetAsync(st.d_u + 16, 0, 4, s));
                 k_pair_eval<<<grid_for(ncand, 128), 128, 0, s>>>(ncand, d_cp1, d_cand, ctree.vel, ct, st.slot_of_key, st.cp, hill_mode,
                                                                  d_code, d_p2, d_sq, d_sest, d_sof, st.d_u + 16);
                 PLAN_CUDA(cudaMemcpyAsync(&nsaddle, st.d_u + 16, 4, cudaMemcpyDeviceToHost, s));
                 rc = st.sync();
                 if (rc) return rc;
-                c.launches += 2;
+                c.launches += 3;
                 if (nsaddle) {
                     rc = launch_density_at(c, d_sq, d_sest, nsaddle, p.knn, d_sden, s);
                     if (rc) return rc;
                     k_saddle_apply<<<grid_for(nsaddle, 128), 128, 0, s>>>(nsaddle, d_sof, d_sden, 2.5 * thr, d_code);
                     c.launches++;
                 }
+                k_flag_resolve<<<grid_for(ncand, 256), 256, 0, s>>>(ncand, d_code, d_rfl);
+                const size_t sb3 = scan_u32_scratch_bytes(ncand + 1), sm3 = c.scratch.used;
+                void *scr3 = c.scratch.take(sb3);
+                if (!scr3) return kErrOutOfMemory;
+                rc = scan_u32(d_rfl, d_rpos, ncand, d_nrl, scr3, sb3, s);
+                c.scratch.used = sm3;
+                if (rc) return rc;
+                k_scatter_flagged<<<grid_for(ncand, 256), 256, 0, s>>>(ncand, d_rfl, d_rpos, d_rlist);
+                c.launches += 4;
             }
+            trace.fine("  candidate pairs evaluated (candidates, saddles)", ncand, nsaddle);
+            trace.fine("  saddle queries with distance ties so far", (long long)c.counters[27]);
             // serial resolution
             PLAN_CUDA(cudaMemsetAsync(st.d_u + 1, 0, 4, s));
-            k_resolve<<<1, 1, 0, s>>>(C, ct, d_cnt, d_off, d_code, d_p2, d_pairs, st.d_u + 1, d_del, st.d_u + 0, st.d_u + 2);
+            k_resolve<<<1, 32, 0, s>>>(d_rlist, d_nrl, d_cp1, ct, d_code, d_p2, d_pairs, st.d_u + 1, d_del, st.d_u + 0, st.d_u + 2);
             c.launches++;
             uint32_t h_u[3];
             PLAN_CUDA(cudaMemcpyAsync(h_u, st.d_u, 12, cudaMemcpyDeviceToHost, s));
@@ -2124,6 +2185,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                 for (uint32_t k = 0; k < npairs; ++k) std::fprintf(stderr, "merge kind %d pred %u prey %u\n", kind, hk[hp[2 * k]], hk[hp[2 * k + 1]]);
             }
             merged_any = npairs > 0;
+            trace.fine("  resolved (pairs)", npairs);
             if (npairs) {
                 PLAN_CUDA(cudaMemsetAsync(d_wave, 0xff, (size_t)(C + 1) * 4, s));
                 k_waves<<<1, 1, 0, s>>>(npairs, d_pairs, C, d_wave, d_pl, d_pf, d_pc, d_pw, st.d_u + 20, st.d_u + 21);
@@ -2153,6 +2215,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                     }
                 }
             }
+            trace.fine("  merged");
             // post-sweep diffuse test with the default tolerance (src/tree.hpp:3984-3992)
             std::vector<uint32_t> masked;
             rc = st.live_order(masked, true);
@@ -2416,6 +2479,8 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                 ra.reach = reach;
                 ra.cp = st.cp;
                 ra.err = c.d_err;
+                // a blocker's calls take longer on larger snapshots: the bound grows with them
+                ra.wait_limit = (uint32_t)std::min<uint64_t>(0xffffffffull, (uint64_t)kWaitLimit * std::max<uint64_t>(1, (Tu + (1u << 24) - 1) >> 24));
                 const unsigned grid = (unsigned)std::min<size_t>(todo.size(), (size_t)rb_grid);
                 double t_a = wall_ms();
                 if (c.kev[0]) cudaEventRecord(c.kev[0], s);
@@ -2632,7 +2697,8 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                                      (unsigned)pass, active_all.size(), calls, acc, w[0], w[13], w[1], w[2], w[12], w[10], w[3] / 1000, w[4] / 1000,
                                      w[14] / 1000, w[15] / 1000, w[16] / 1000, w[5] / 1000, w[6] / 1000, w[8] / 1000, w[9] / 1000, w[7], w[11]);
                         for (int q = 0; q < 7; ++q) std::fprintf(stderr, " %llu/%llu", w[17 + q], w[24 + q] / 1000);
-                        std::fprintf(stderr, "\n");
+                        std::fprintf(stderr, " | tiles %llu set-up kcycles %llu; predicted %llu held %llu taken %llu\n", w[32], w[31] / 1000, w[33],
+                                     w[34], w[35]);
                     }
                 }
             }

@@ -10,8 +10,10 @@
 // one collecting traversal at the final radius that feeds a heap with the library's
 // sifting order, so ties resolve as in the reference. FP64 throughout, no contraction.
 #include <cmath>
+#include <cstdlib>
 #include <type_traits>
 
+#include "exact64.cuh"
 #include "pipeline.h"
 #include "tree_walk.cuh"
 #include "knn_f32.cuh"
@@ -84,14 +86,16 @@ __global__ void __launch_bounds__(128) k_knn_positions(KTree t, const double *q3
 }
 
 
+// exact heap path, thread per query; list: the queries to answer (null: all nq)
 template <int KMAX, int SPL>
-__global__ void __launch_bounds__(128) k_density_at(KTree t, const double *q3, const double *est, uint32_t nq, uint32_t k,
+__global__ void __launch_bounds__(128) k_density_at(KTree t, const double *q3, const double *est, const uint32_t *list, uint32_t nq, uint32_t k,
                                                     double four_pi_over_three, SplineCells sc, double *out, unsigned *err) {
     extern __shared__ unsigned char smem[];
     double *sd = reinterpret_cast<double *>(smem);
     uint32_t *si = reinterpret_cast<uint32_t *>(sd + KMAX * blockDim.x);
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nq) return;
+    if (list) i = list[i];
     SlabHeap h{sd + threadIdx.x, si + threadIdx.x, (int)blockDim.x};
     double qx = q3[3 * i], qy = q3[3 * i + 1], qz = q3[3 * i + 2];
     double r = est[i] != 0 ? est[i] : knn_first_radius(t, qx, qy, qz, 0xffffffffu, k, err);
@@ -104,6 +108,132 @@ __global__ void __launch_bounds__(128) k_density_at(KTree t, const double *q3, c
         out[i] = spline_density(t.pos, [&](int j) { return h.iget(j); }, (int)k, p0.x, p0.y, p0.z, sc);
     } else {
         out[i] = knn_median_density(t, h, (int)k, four_pi_over_three);
+    }
+}
+
+// Ascending sort of (key, index) pairs [0, n) by one warp (bitonic, in shared memory; the
+// entries up to the next power of two are padded, so C, a power of two, bounds n).
+template <int C>
+__device__ inline void warp_sort_pairs(unsigned long long *key, uint32_t *ix, uint32_t n, int lane) {
+    uint32_t P = 1;
+    while (P < n) P <<= 1;
+    for (uint32_t j = n + lane; j < P; j += 32) {
+        key[j] = ~0ull;
+        ix[j] = 0xffffffffu;
+    }
+    __syncwarp();
+    for (uint32_t size = 2; size <= P; size <<= 1)
+        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+            for (uint32_t u = lane; u < P / 2; u += 32) {
+                const uint32_t a = 2 * u - (u & (stride - 1)), b = a + stride;
+                const bool up = (a & size) == 0;
+                const unsigned long long ka = key[a], kb = key[b];
+                const uint32_t ia = ix[a], ib = ix[b];
+                const bool gt = ka > kb || (ka == kb && ia > ib);
+                if (gt == up) {
+                    key[a] = kb;
+                    key[b] = ka;
+                    ix[a] = ib;
+                    ix[b] = ia;
+                }
+            }
+            __syncwarp();
+        }
+}
+
+// Warp-cooperative form of k_density_at for queries that visit many points (the saddle
+// tests of the merge sweeps reach 10^5 points and more): one warp per query walks the tree
+// exactly as the reference does (every lane on the same path), the lanes take 32 points of
+// a visited range at a time, and every point within the running k-th smallest squared
+// distance goes to a per-warp buffer that a warp sort compacts. A squared distance is
+// non-negative, so its bits order like its value. With no tie at the k-boundary or inside
+// the k-set, the k kept are the reference heap's contents in its sorted order; a query with
+// such a tie, or one whose ties overflow the buffer, is listed for the exact heap path.
+template <int KM, int SPL>
+__global__ void __launch_bounds__(128) k_density_at_w(KTree t, const double *q3, const double *est, uint32_t nq, uint32_t k, double fpo3,
+                                                      SplineCells sc, double *out, uint32_t *redo, uint32_t *nredo, unsigned *err) {
+    constexpr uint32_t C = 4 * KM;  // candidates per warp
+    __shared__ unsigned long long s_key[4][C];
+    __shared__ uint32_t s_ix[4][C];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const uint32_t i = blockIdx.x * 4 + w;
+    if (i >= nq) return;
+    const unsigned full = 0xffffffffu;
+    unsigned long long *key = s_key[w];
+    uint32_t *ix = s_ix[w];
+    const double qx = q3[3 * i], qy = q3[3 * i + 1], qz = q3[3 * i + 2];
+    double r = est[i] != 0 ? est[i] : knn_first_radius(t, qx, qy, qz, 0xffffffffu, k, err);
+    r = knn_final_radius(t, qx, qy, qz, r, k, err);
+    uint32_t n = 0, visited = 0;     // buffered candidates, points visited (the same in every lane)
+    unsigned long long tau = ~0ull;  // the running k-th smallest (bits); a point above it is out
+    bool overflow = false;
+    auto compact = [&]() {
+        warp_sort_pairs<C>(key, ix, n, lane);
+        if (n >= k) {
+            tau = key[k - 1];
+            uint32_t m = k;
+            while (m < n && key[m] == tau) ++m;
+            n = m;
+        }
+    };
+    traverse(t, qx, qy, qz, r,
+             [&](uint32_t b, uint32_t e, bool) {
+                 for (uint32_t p0 = b; p0 < e; p0 += 32) {
+                     const uint32_t p = p0 + (uint32_t)lane;
+                     unsigned long long kb = ~0ull;
+                     if (p < e) kb = dbits(point_dr2(qx, qy, qz, t.pos[p]));
+                     unsigned m = __ballot_sync(full, p < e && kb <= tau);
+                     if (!m) continue;
+                     if (n + __popc(m) > C) {
+                         compact();
+                         m = __ballot_sync(full, p < e && kb <= tau);
+                         if (n + __popc(m) > C) {
+                             overflow = true;
+                             return false;
+                         }
+                     }
+                     if ((m >> lane) & 1u) {
+                         const uint32_t at = n + __popc(m & ((1u << lane) - 1u));
+                         key[at] = kb;
+                         ix[at] = p;
+                     }
+                     n += __popc(m);
+                     __syncwarp();
+                 }
+                 visited += e - b;
+                 return true;
+             },
+             err);
+    bool redo_it = overflow;
+    if (!redo_it) {
+        compact();
+        if (visited < k) {  // fewer points than neighbours: the reference's zero
+            if (lane == 0) out[i] = 0.0;
+            return;
+        }
+        bool tie = n > k;  // a point beyond the k-th at the same distance
+        for (uint32_t j = 1 + (uint32_t)lane; j < k; j += 32) tie = tie || key[j] == key[j - 1];
+        redo_it = __any_sync(full, tie);
+    }
+    if (redo_it) {
+        if (lane == 0) redo[atomicAdd(nredo, 1u)] = i;
+        return;
+    }
+    if (lane == 0) {
+        if constexpr (SPL) {
+            const double4_32a p0 = t.pos[0];  // self_id = 0, as in the exact path
+            out[i] = spline_density(t.pos, [&](int j) { return ix[j]; }, (int)k, p0.x, p0.y, p0.z, sc);
+        } else {
+            // MedianSphericalDensityKernel on the sorted k-set, as knn_median_density
+            int j = (int)k;
+            const double m2 = 4 * dfrom(key[j / 2]);
+            for (j = j - 1; j >= 0; j--)
+                if (!(dfrom(key[j]) > m2)) break;
+            const double r2 = dfrom(key[j]);
+            double dens = 0;
+            for (; j >= 0; j--) dens = dens + t.pos[ix[j]].w;
+            out[i] = dens / (fpo3 * cr_pow15(r2));
+        }
     }
 }
 
@@ -361,15 +491,42 @@ int launch_density_at(Context &c, const double *d_q3, const double *d_est, uint3
     if (nq == 0) return kOk;
     KTree t = ktree_of(c.tree);
     const double fpo3 = 3.14159265358979323846 * 4. / 3.;
-    return launch_by_k(k, [&](auto km, int threads) {
+    const bool spl = !c.fs.median_kernel;
+    const size_t mark = c.scratch.used;
+    uint32_t *redo = c.scratch.get<uint32_t>(nq + 1), *nredo = c.scratch.get<uint32_t>(4);
+    if (!redo || !nredo) {
+        c.scratch.used = mark;
+        return kErrOutOfMemory;
+    }
+    PLAN_CUDA(cudaMemsetAsync(nredo, 0, 4, s));
+    // a warp per query; the queries with distance ties go to the exact heap path
+    int rc = launch_by_k(k, [&](auto km, int) {
         constexpr int KM = decltype(km)::value;
-        size_t sm = (size_t)KM * threads * 12;
-        auto kern = c.fs.median_kernel ? k_density_at<KM, 0> : k_density_at<KM, 1>;
-        kern<<<grid_for(nq, threads), threads, sm, s>>>(t, d_q3, d_est, nq, k, fpo3, c.fs.spline, d_out, c.d_err);
+        auto kern = spl ? k_density_at_w<KM, 1> : k_density_at_w<KM, 0>;
+        kern<<<(nq + 3) / 4, 128, 0, s>>>(t, d_q3, d_est, nq, k, fpo3, c.fs.spline, d_out, redo, nredo, c.d_err);
         c.launches++;
         PLAN_CUDA(cudaGetLastError());
         return (int)kOk;
     });
+    uint32_t h = 0;
+    if (!rc) {
+        PLAN_CUDA(cudaMemcpyAsync(&h, nredo, 4, cudaMemcpyDeviceToHost, s));
+        PLAN_CUDA(cudaStreamSynchronize(s));
+        c.counters[27] += h;
+    }
+    if (!rc && h)
+        rc = launch_by_k(k, [&](auto km, int threads) {
+            constexpr int KM = decltype(km)::value;
+            size_t sm = (size_t)KM * threads * 12;
+            auto kern = spl ? k_density_at<KM, 1> : k_density_at<KM, 0>;
+            kern<<<grid_for(h, threads), threads, sm, s>>>(t, d_q3, d_est, redo, h, k, fpo3, c.fs.spline, d_out, c.d_err);
+            c.launches++;
+            PLAN_CUDA(cudaGetLastError());
+            return (int)kOk;
+        });
+    if (h) PLAN_CUDA(cudaStreamSynchronize(s));  // the redo list is scratch, released here
+    c.scratch.used = mark;
+    return rc;
 }
 
 int knn_positions(Context &c, const double *pos3, uint32_t nq, uint32_t k, double est, uint32_t *idx, double *dr2) {

@@ -183,7 +183,7 @@ __device__ inline double warp_ordered_sum_window(const double (&x)[K], uint32_t 
         // the first remaining term of this lane whose partial sum leaves the binade (stop at
         // it) or lands on its upper edge (stop after it)
         int stop = K;
-        bool stopped = false;
+        bool stopped = false, edge = false;
         long long run = n0 + before;
 #pragma unroll
         for (int j = 0; j < K; ++j) {
@@ -199,12 +199,14 @@ __device__ inline double warp_ordered_sum_window(const double (&x)[K], uint32_t 
                 } else if (an == (1LL << 53)) {
                     stop = j + 1;
                     stopped = true;
+                    edge = true;
                 }
             }
         }
         const unsigned hit = __ballot_sync(full, stopped);
         const int L = hit ? __ffs(hit) - 1 : 31;
         const int stopL = __shfl_sync(full, stop, L);
+        const bool edgeL = __shfl_sync(full, edge ? 1 : 0, L) != 0;
         const uint32_t end = min(cnt, (uint32_t)(L * K + stopL));  // terms [pos, end) fit the grid
         if (end > pos) {
             // the grid integer of the partial sum after term end - 1
@@ -218,8 +220,10 @@ __device__ inline double warp_ordered_sum_window(const double (&x)[K], uint32_t 
             val = __shfl_sync(full, val, (int)ll);
             s = grid_value(val, ex);
             pos = end;
-        } else {
-            // the first remaining term does not fit the grid: one ordinary add
+        }
+        if (hit && !edgeL) {
+            // term pos does not fit the grid of s (whose binade is unchanged by the run): one
+            // ordinary add, which a new step would also take, since its grid is the same
             double v = 0.0;
 #pragma unroll
             for (int j = 0; j < K; ++j)

@@ -38,9 +38,9 @@ constexpr int kRB = 512;                      // threads of a rebinding block
 constexpr int kRbWarps = kRB / 32;
 constexpr uint32_t kRbFront = 4096;           // frontier entries of the ball search
 constexpr uint32_t kRbSmall = 4096;           // members sorted in shared memory
-constexpr uint32_t kWaitLimit = 1u << 25;     // bounded waits on blockers (about 30 s)
+constexpr uint32_t kWaitLimit = 1u << 25;     // bounded waits on blockers: sleeps of 1 us per 2^24 points
 constexpr uint32_t kCallLimit = 1u << 20;     // calls of one clump in one launch
-constexpr int kRbStats = 32;                  // counters per slot
+constexpr int kRbStats = 40;                  // counters per slot
 // dynamic shared memory: the largest of the frontier, the small sort and the acceptance
 // tile (per candidate: FP64 position and velocity, index, FP32 form, taken flag)
 constexpr size_t kRbTileBytes = (size_t)kRB * (64 + 4 + sizeof(CandF) + 1);
@@ -76,6 +76,7 @@ struct RbArgs {
     unsigned long long *reach;
     CP cp;
     unsigned *err;
+    uint32_t wait_limit;   // sleeps a block waits for one blocker before it reports an error
 };
 
 // per-point products for the member sums (src/tree.hpp:4436-4440: mass, pos * mass,
@@ -301,6 +302,9 @@ __device__ uint32_t rb_call(const RbArgs &a, uint32_t slot, uint32_t myrank, RbS
         sh.u[13] = 0;
         sh.u[14] = 0;
         sh.u[15] = 0;
+        sh.u[16] = 0;
+        sh.u[17] = 0;
+        sh.u[18] = 0;
     }
     if (tid < 32) {
         comp = lane < 6 ? sh.st[1 + lane] : 0.0;
@@ -416,7 +420,10 @@ __device__ uint32_t rb_call(const RbArgs &a, uint32_t slot, uint32_t myrank, RbS
         nph = a.ft.phi[nq];
         npl = a.ft.plo[nq];
     }
+    long long t_setup = 0;
+    uint32_t n_tiles = 0;
     for (uint32_t base = 0; base < nel; base += kRB) {
+        const long long tt0 = clock64();
         const uint32_t q = nq;
         const uint32_t tlen = min((uint32_t)kRB, nel - base);
         const bool valid = q != kNone;
@@ -432,6 +439,11 @@ __device__ uint32_t rb_call(const RbArgs &a, uint32_t slot, uint32_t myrank, RbS
                 tn = kNone;
             }
             taken = (ow != kNone && ow <= myrank) || (tn != kNone && tn < myrank);
+            if (stat) {
+                if (tn != kNone && tn < myrank) atomicAdd(&sh.u[16], 1u);
+                if (ow != kNone && ow < myrank) atomicAdd(&sh.u[17], 1u);
+                if (taken) atomicAdd(&sh.u[18], 1u);
+            }
             if (ow != kNone && ow < myrank)
                 defer_add(a.dset, a.dover, a.dmax, slot, ow, *(volatile const uint8_t *)&a.finished[a.slot_of_rank[ow]] == 0);
             else if (tn != kNone && tn < myrank)
@@ -460,6 +472,8 @@ __device__ uint32_t rb_call(const RbArgs &a, uint32_t slot, uint32_t myrank, RbS
             npl = a.ft.plo[nq];
         }
         __syncthreads();
+        t_setup += clock64() - tt0;
+        ++n_tiles;
         for (uint32_t pos = 0;;) {
             ++rounds;
             bool bound = false, unsure = false;
@@ -543,6 +557,11 @@ __device__ uint32_t rb_call(const RbArgs &a, uint32_t slot, uint32_t myrank, RbS
             stat[14] += sh.u[13];
             stat[15] += sh.u[14];  // of which the table look-up / rebuild
             stat[16] += sh.u[15];  // and the FP64 update chain
+            stat[31] += (unsigned long long)t_setup;  // tile set-up: loads arriving, filters, splits
+            stat[32] += n_tiles;
+            stat[33] += sh.u[16];  // candidates predicted for an earlier clump
+            stat[34] += sh.u[17];  // held by an earlier clump
+            stat[35] += sh.u[18];  // taken either way
         }
         if (nacc) {
             a.ct.moff[slot] = no;
@@ -643,37 +662,62 @@ __device__ bool rb_sort_particles(const RbArgs &a, uint32_t slot, RbShared &sh, 
     uint32_t *idx = a.P.idx + o;
     double *dist = a.P.dist + o;
     // 1) the seven sums in member order (CalculateKinematicProperties): warp w < 7 runs sum w
-    // over the per-point products, 128 terms per step; the member indices of the window
-    // after next and the terms of the next window are loaded while a window is summed
+    // over the per-point products, 64 terms per step, from a shared-memory stage that the
+    // other nine warps fill: 256 members at a time (one per loading thread), double-buffered,
+    // the member indices of a chunk read one chunk ahead, so the sums never wait on a gather
+    // from memory
     double acc = 0.0;
     uint32_t its = 0;
     long long tsum = 0;
-    if (wid < 7) {
-        const long long ts = clock64();
-        const double *tsrc = wid < 4 ? reinterpret_cast<const double *>(a.tm0) + wid : reinterpret_cast<const double *>(a.tm1) + (wid - 4);
-        constexpr int kK = 2;  // terms per lane and window
-        constexpr uint32_t kW = 32 * kK;
-        uint32_t qa[kK], qb[kK];
-        double x[kK], nx[kK];
-#pragma unroll
-        for (int j = 0; j < kK; ++j) {
-            const uint32_t k = (uint32_t)lane * kK + j;
-            qa[j] = k < m ? idx[k] : 0u;
-            qb[j] = kW + k < m ? idx[kW + k] : 0u;
+    {
+        constexpr uint32_t kCh = 256;            // members per chunk
+        constexpr uint32_t kLd = kRB - 7 * 32;   // loading threads (warps 7..15)
+        constexpr int kK = 2;                    // terms per lane and step
+        static_assert(2 * 7 * kCh * sizeof(double) <= kRbSmem, "sum stage");
+        static_assert(kCh <= kLd && kCh % (32 * kK) == 0, "sum chunk");
+        double *stg = reinterpret_cast<double *>(sh.buf);  // [2][7][kCh]
+        auto put = [&](double *d, uint32_t k, const double4_32a &p, const double4_32a &v) {
+            d[k] = p.x;
+            d[kCh + k] = p.y;
+            d[2 * kCh + k] = p.z;
+            d[3 * kCh + k] = p.w;
+            d[4 * kCh + k] = v.x;
+            d[5 * kCh + k] = v.y;
+            d[6 * kCh + k] = v.z;
+        };
+        const uint32_t nch = (m + kCh - 1) / kCh;
+        if ((uint32_t)tid < min(m, kCh)) {  // chunk 0: every thread
+            const uint32_t q = idx[tid];
+            put(stg, (uint32_t)tid, a.tm0[q], a.tm1[q]);
         }
-#pragma unroll
-        for (int j = 0; j < kK; ++j) x[j] = (uint32_t)lane * kK + j < m ? tsrc[4 * (size_t)qa[j]] : 0.0;
-        for (uint32_t base = 0; base < m; base += kW) {
-#pragma unroll
-            for (int j = 0; j < kK; ++j) {
-                const uint32_t k = base + kW + (uint32_t)lane * kK + j;
-                nx[j] = k < m ? tsrc[4 * (size_t)qb[j]] : 0.0;
-                const uint32_t k2 = k + kW;
-                qb[j] = k2 < m ? idx[k2] : 0u;
+        const uint32_t k0 = (uint32_t)tid - 7u * 32u;  // loading threads: their member of a chunk
+        uint32_t q0 = 0;                              // and its index in the next chunk
+        if (wid >= 7 && k0 < kCh && kCh + k0 < m) q0 = idx[kCh + k0];
+        __syncthreads();
+        const long long ts = clock64();
+        for (uint32_t c = 0; c < nch; ++c) {
+            const uint32_t b = c & 1u;
+            if (wid < 7) {
+                const double *src = stg + ((size_t)b * 7 + wid) * kCh;
+                const uint32_t cnt = min(kCh, m - c * kCh);
+                for (uint32_t w0 = 0; w0 < cnt; w0 += 32 * kK) {
+                    const uint32_t k = w0 + (uint32_t)lane * kK;
+                    double x[kK];
+                    const double2 v2 = k < cnt ? *reinterpret_cast<const double2 *>(src + k) : make_double2(0.0, 0.0);
+                    x[0] = v2.x;
+                    x[1] = k + 1 < cnt ? v2.y : 0.0;
+                    acc = warp_ordered_sum_window<kK>(x, min(32u * kK, cnt - w0), acc, &its);
+                }
+            } else if (c + 1 < nch && k0 < kCh) {
+                // chunk c + 1 into the other buffer, and the index of chunk c + 2
+                const uint32_t g1 = (c + 1) * kCh, g2 = g1 + kCh;
+                if (g1 + k0 < m) {
+                    const double4_32a p0 = a.tm0[q0], u0 = a.tm1[q0];
+                    q0 = g2 + k0 < m ? idx[g2 + k0] : 0u;
+                    put(stg + (size_t)(b ^ 1u) * 7 * kCh, k0, p0, u0);
+                }
             }
-            acc = warp_ordered_sum_window<kK>(x, min(kW, m - base), acc, &its);
-#pragma unroll
-            for (int j = 0; j < kK; ++j) x[j] = nx[j];
+            __syncthreads();
         }
         tsum = clock64() - ts;
     }
@@ -852,7 +896,7 @@ __device__ bool rb_sort_particles(const RbArgs &a, uint32_t slot, RbShared &sh, 
 __global__ void __launch_bounds__(kRB, 1) k_rebind_loop(RbArgs a) {
     extern __shared__ __align__(16) unsigned char rb_dyn[];
     __shared__ uint32_t warp_tot[kRbWarps];
-    __shared__ uint32_t u[16];
+    __shared__ uint32_t u[20];
     __shared__ double st[8], tabM[32], tabY[32], sd[8];
     __shared__ float tabF[32], sf[16];
     __shared__ uint32_t s_item;
@@ -869,7 +913,7 @@ __global__ void __launch_bounds__(kRB, 1) k_rebind_loop(RbArgs a) {
             for (uint32_t b = a.blk_off[item]; b < a.blk_off[item + 1]; ++b) {
                 const uint32_t bs = a.blk[b];
                 for (uint32_t it = 0; *(volatile uint8_t *)&a.finished[bs] == 0; ++it) {
-                    if (it >= kWaitLimit) {
+                    if (it >= a.wait_limit) {
                         atomicOr(a.err, (unsigned)kDevErrLoopLimit);
                         break;
                     }

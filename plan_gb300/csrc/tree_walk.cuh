@@ -159,8 +159,9 @@ __device__ inline double knn_first_radius(const KTree &t, double qx, double qy, 
 
 // One KNN query: returns the number of kept neighbours (k unless the tree is smaller) in
 // the heap slab, sorted ascending by dr2.
-__device__ inline int knn_query(const KTree &t, double qx, double qy, double qz, double r, uint32_t k, SlabHeap &h, unsigned *err) {
-    // radius doubling with count-only passes (the reference refills its heap per radius)
+// The radius of the collecting pass: doubled from r until the nodes the sphere contains or
+// meets hold at least k points (count-only passes; the reference refills its heap per radius).
+__device__ inline double knn_final_radius(const KTree &t, double qx, double qy, double qz, double r, uint32_t k, unsigned *err) {
     for (int it = 0; it < 200; ++it) {
         uint32_t cnt = 0;
         traverse(t, qx, qy, qz, r, [&](uint32_t b, uint32_t e, bool) { cnt += e - b; return cnt < k; }, err);
@@ -168,10 +169,24 @@ __device__ inline int knn_query(const KTree &t, double qx, double qy, double qz,
         r = r * 2;
         if (it == 199) atomicOr(err, (unsigned)kDevErrLoopLimit);
     }
+    return r;
+}
+
+__device__ inline int knn_query(const KTree &t, double qx, double qy, double qz, double r, uint32_t k, SlabHeap &h, unsigned *err) {
+    r = knn_final_radius(t, qx, qy, qz, r, k, err);
     int size = 0;
     traverse(t, qx, qy, qz, r,
              [&](uint32_t b, uint32_t e, bool) {
-                 for (uint32_t p = b; p < e; ++p) h.add(size, (int)k, p, point_dr2(qx, qy, qz, t.pos[p]));
+                 // eight points loaded together, then added in order: the loads overlap
+                 uint32_t p = b;
+                 for (; p + 8 <= e; p += 8) {
+                     double d[8];
+#pragma unroll
+                     for (int j = 0; j < 8; ++j) d[j] = point_dr2(qx, qy, qz, t.pos[p + j]);
+#pragma unroll
+                     for (int j = 0; j < 8; ++j) h.add(size, (int)k, p + j, d[j]);
+                 }
+                 for (; p < e; ++p) h.add(size, (int)k, p, point_dr2(qx, qy, qz, t.pos[p]));
                  return true;
              },
              err);
