@@ -56,7 +56,7 @@ REBIND_BYTES_PER_MEMBER = 28
 # dram bytes read + written per unit, measured with ncu on smaller snapshots of the same
 # mixture (profiles/k_rebind_loop_workload2.md, profiles/k_density_f_workload2.md); traffic grows with
 # the units processed, so a full-size launch's traffic is taken as units times these figures
-REBIND_TRAFFIC_PER_MEMBER = (167_780_608 + 45_761_280) / 260_562    # first launch, 1M snapshot: 819.5 B
+REBIND_TRAFFIC_PER_MEMBER = (642_154_240 + 417_524_992) / 662_193    # first launch, 1M snapshot: 1,600 B
 DENSITY_TRAFFIC_PER_POINT = (928_974_848 + 483_069_184) / 6_736_104  # 4M snapshot: 209.6 B
 # the catalogue of the benchmarked snapshot as the unmodified reference writes it
 # (tests/golden/w2_16m, made by tests/golden/make_golden.py)
