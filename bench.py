@@ -17,7 +17,8 @@ path); value is the particles of all ranks over the slowest rank's time.
 
 `--impl reference` times the CPU restatement of the same path (oracle/, the reference's
 algorithm; the reference program itself is not built where this runs) with all host
-cores on a bounded sample of the same workload, and prints the same JSON line.
+cores on the same full snapshot, pass after pass until --steps are done or --ref-budget
+seconds have run, and prints the same JSON line.
 """
 from __future__ import annotations
 
