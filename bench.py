@@ -62,6 +62,8 @@ DENSITY_TRAFFIC_PER_POINT = (928_974_848 + 483_069_184) / 6_736_104  # 4M snapsh
 # the catalogue of the benchmarked snapshot as the unmodified reference writes it
 # (tests/golden/w2_16m, made by tests/golden/make_golden.py)
 GOLDEN_FULL = ROOT / "tests" / "golden" / "w2_16m" / "meta.json"
+# the reference's catalogues recorded for other sizes of the same mixture (seed 1)
+GOLDEN_BY_N = {N_FULL: GOLDEN_FULL, 1 << 27: ROOT / "tests" / "golden" / "w2_134m" / "meta.json"}
 
 
 def _peaks() -> tuple[float, str]:
@@ -265,13 +267,15 @@ def run_reference(args) -> None:
 
 
 def check_parity(cat, n: int, seed: int):
-    """The catalogue against the reference's for the benchmarked snapshot: the summary line and
-    the SHA-256 of peaks_at_*.txt must be equal. None for snapshots without a recorded one."""
+    """The catalogue against the reference's for the benchmarked snapshot (and the 2^27 one):
+    the summary line and the SHA-256 of peaks_at_*.txt must be equal. None for snapshots
+    without a recorded one."""
     import hashlib
 
-    if n != N_FULL or seed != SEED or not GOLDEN_FULL.exists():
+    gf = GOLDEN_BY_N.get(n)
+    if seed != SEED or gf is None or not gf.exists():
         return None
-    g = json.loads(GOLDEN_FULL.read_text())
+    g = json.loads(gf.read_text())
     with tempfile.TemporaryDirectory() as d:
         cat.write_peaks(str(Path(d) / "res.txt"))
         got = hashlib.sha256((Path(d) / g["peaks_file"]).read_bytes()).hexdigest()

@@ -991,8 +991,14 @@ __device__ __forceinline__ void split_f(double d, float &hi, float &lo) {
 constexpr int kDeferSlots = 16;
 constexpr uint32_t kDeferSpec = 0x80000000u;
 
-__device__ void defer_add(uint32_t *dset, uint8_t *dover, uint32_t *dmax, uint32_t slot, uint32_t ow, bool spec = true) {
-    atomicMax(&dmax[slot], ow + 1);
+// dcall (may be null): per record, the call of the clump's run (1-based, counted from its
+// state before rebinding) in which the record was made; a clump's calls run in order, so
+// that is the earliest call that skipped such a particle. dfirst: the earliest call of any
+// deferral, kept also when the records overflow. A rerun may resume after those calls.
+__device__ void defer_add(uint32_t *dset, uint8_t *dover, uint32_t *dmax, uint32_t slot, uint32_t ow, bool spec = true,
+                          uint32_t *dcall = nullptr, uint32_t *dfirst = nullptr, uint32_t call = kNone) {
+    if (*(volatile uint32_t *)&dmax[slot] < ow + 1) atomicMax(&dmax[slot], ow + 1);
+    if (dfirst && call < *(volatile uint32_t *)&dfirst[slot]) atomicMin(&dfirst[slot], call);
     const uint32_t rec = ow | (spec ? kDeferSpec : 0u);
     uint32_t *d = dset + (size_t)slot * kDeferSlots;
     for (int j = 0; j < kDeferSlots; ++j) {
@@ -1000,6 +1006,7 @@ __device__ void defer_add(uint32_t *dset, uint8_t *dover, uint32_t *dmax, uint32
         if (v == rec) return;
         if (v == kNone) {
             const uint32_t old = atomicCAS(&d[j], kNone, rec);
+            if (old == kNone && dcall) atomicMin(&dcall[(size_t)slot * kDeferSlots + j], call);
             if (old == kNone || old == rec) return;
         }
     }
@@ -1469,53 +1476,141 @@ __global__ void __launch_bounds__(kRebindThreads) k_rebind_round(const uint32_t 
     }
 }
 
-// restore listed clumps to their state before rebinding (segments re-materialised from the
-// saved pool) and clear their per-pass records
-__global__ void k_rebind_restore(const uint32_t *list, uint32_t n, CT ct, Pool P, const double *bM, const double *bh, const double *bri,
-                                 const double *bro, const double *br10, const double *br2, const double4_32a *bc, const double4_32a *bv,
-                                 const uint32_t *bo, const uint32_t *bn, const uint32_t *bidx, const double *bdist, uint8_t *invalid,
-                                 uint32_t *dmax, uint32_t *dset, uint8_t *dover, unsigned *err) {
-    __shared__ uint32_t s_off;
+// What k_rebind_restore needs beyond the clump table and the pool.
+struct RestoreArgs {
+    const double *bM, *bh, *bri, *bro, *br10, *br2;  // the state before rebinding, per slot
+    const double4_32a *bc, *bv;
+    const uint32_t *bo, *bn, *bidx;
+    const double *bdist;
+    uint8_t *invalid, *dover, *distsq, *needsort;
+    uint32_t *dmax, *dset, *dcall, *dfirst, *ccall, *owner;
+    const uint32_t *keep, *rank_of;  // keep (by list position, may be null): checkpoints kept
+    const uint8_t *in_clump;
+    Ckpt ck;                         // ck.n null: no checkpoints
+};
+
+// Restore listed clumps for a rerun: to their state before rebinding, or, when the first
+// call the rerun affects comes after some of their checkpoints, to the last of those (its
+// members claimed again, the deferral records of the calls before it kept, the rest
+// cleared); either way the per-pass records of later calls go.
+__global__ void k_rebind_restore(const uint32_t *list, uint32_t n, CT ct, Pool P, RestoreArgs r, unsigned *err) {
+    __shared__ uint32_t s_off, s_m, s_kp, s_rank;
+    __shared__ const uint32_t *s_idx;
+    __shared__ const double *s_dist;
     uint32_t t = blockIdx.x;
     if (t >= n) return;
     uint32_t sl = list[t];
     if (threadIdx.x == 0) {
-        ct.M[sl] = bM[sl]; ct.hill[sl] = bh[sl]; ct.r_in[sl] = bri[sl]; ct.r_out[sl] = bro[sl]; ct.r10[sl] = br10[sl]; ct.r2s[sl] = br2[sl];
-        ct.com[sl] = bc[sl]; ct.vcom[sl] = bv[sl];
-        s_off = pool_alloc(P, bn[sl], err);
-        invalid[sl] = 0;
-        dmax[sl] = 0;
-        dover[sl] = 0;
-        for (int j = 0; j < kDeferSlots; ++j) dset[(size_t)sl * kDeferSlots + j] = kNone;
+        const uint32_t kp = (r.keep && r.ck.n) ? r.keep[t] : 0u;
+        const uint32_t rank = r.rank_of[sl];
+        ct.r_in[sl] = r.bri[sl]; ct.r_out[sl] = r.bro[sl]; ct.r10[sl] = r.br10[sl]; ct.r2s[sl] = r.br2[sl];
+        uint32_t lim = 0;  // calls kept
+        if (kp == 0) {
+            ct.M[sl] = r.bM[sl]; ct.hill[sl] = r.bh[sl];
+            ct.com[sl] = r.bc[sl]; ct.vcom[sl] = r.bv[sl];
+            s_idx = r.bidx + r.bo[sl];
+            s_dist = r.bdist + r.bo[sl];
+            s_m = r.bn[sl];
+        } else {
+            const size_t e = (size_t)rank * kCk + (kp - 1);
+            const double *q = r.ck.st + e * 8;
+            ct.M[sl] = q[0];
+            ct.com[sl] = make_double4_32a(q[1], q[2], q[3], 0);
+            ct.vcom[sl] = make_double4_32a(q[4], q[5], q[6], 0);
+            ct.hill[sl] = q[7];
+            s_idx = r.ck.idx + r.ck.off[e];
+            s_dist = r.ck.dist + r.ck.off[e];
+            s_m = r.ck.m[e];
+            lim = r.ck.call[e];
+            r.distsq[sl] = 1;  // a checkpoint holds the squared distances of its sort
+            r.needsort[sl] = 0;
+        }
+        if (r.ck.n) r.ck.n[rank] = kp;
+        if (r.ccall) r.ccall[sl] = lim;
+        s_kp = kp;
+        s_rank = rank;
+        s_off = pool_alloc(P, s_m, err);
+        r.invalid[sl] = 0;
+        // the records of the kept calls, packed to the front
+        uint32_t w = 0, dm = 0, df = kNone;
+        uint32_t *ds = r.dset + (size_t)sl * kDeferSlots, *dc = r.dcall ? r.dcall + (size_t)sl * kDeferSlots : nullptr;
+        for (int j = 0; j < kDeferSlots; ++j) {
+            const uint32_t v = ds[j], cj = dc ? dc[j] : kNone;
+            if (v != kNone && kp > 0 && cj <= lim) {
+                ds[w] = v;
+                if (dc) dc[w] = cj;
+                dm = max(dm, (v & ~kDeferSpec) + 1);
+                df = min(df, cj);
+                ++w;
+            }
+        }
+        for (int j = (int)w; j < kDeferSlots; ++j) {
+            ds[j] = kNone;
+            if (dc) dc[j] = kNone;
+        }
+        r.dmax[sl] = dm;
+        if (r.dfirst) r.dfirst[sl] = df;
+        r.dover[sl] = 0;
     }
     __syncthreads();
     if (s_off == kNone) return;
-    for (uint32_t k = threadIdx.x; k < bn[sl]; k += blockDim.x) {
-        P.idx[s_off + k] = bidx[bo[sl] + k];
-        P.dist[s_off + k] = bdist[bo[sl] + k];
+    const uint32_t m = s_m;
+    for (uint32_t k = threadIdx.x; k < m; k += blockDim.x) {
+        const uint32_t q = s_idx[k];
+        P.idx[s_off + k] = q;
+        P.dist[s_off + k] = s_dist[k];
+        if (s_kp && !r.in_clump[q]) atomicMin(&r.owner[q], s_rank);  // the checkpoint's holdings
     }
     if (threadIdx.x == 0) {
         ct.moff[sl] = s_off;
-        ct.mn[sl] = bn[sl];
+        ct.mn[sl] = m;
     }
 }
 
 // After a pass: a clump whose accepted particles are not all still its own lost one to an
 // earlier clump (the claims keep the lowest rank); it is invalid and depends on that clump.
+// For an invalid clump, lost_ck (by rank) is the first of its checkpoints that holds a
+// particle it lost: its run is good up to the checkpoint before that one.
 __global__ void k_rebind_verify(const uint32_t *list, uint32_t n, CT ct, Pool P, const uint8_t *in_clump, const uint32_t *owner,
-                                const uint32_t *rank_of, uint8_t *invalid, uint32_t *dset, uint8_t *dover, uint32_t *dmax) {
+                                const uint32_t *rank_of, uint8_t *invalid, uint32_t *dset, uint8_t *dover, uint32_t *dmax, Ckpt ck,
+                                uint32_t *lost_ck) {
+    __shared__ int s_lost;
     if (blockIdx.x >= n) return;
     const uint32_t s = list[blockIdx.x];
     const uint32_t myrank = rank_of[s], o = ct.moff[s], m = ct.mn[s];
+    if (threadIdx.x == 0) s_lost = 0;
+    __syncthreads();
     for (uint32_t k = threadIdx.x; k < m; k += blockDim.x) {
         const uint32_t q = P.idx[o + k];
         if (in_clump[q]) continue;  // a member before rebinding
         const uint32_t w = owner[q];
         if (w != myrank) {
             invalid[s] = 1;
+            s_lost = 1;
             if (w != kNone && w < myrank) defer_add(dset, dover, dmax, s, w);
         }
     }
+    __syncthreads();
+    if (!s_lost || !ck.n) return;
+    const uint32_t nck = ck.n[myrank];
+    uint32_t first = nck;
+    for (uint32_t i = 0; i < nck; ++i) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_lost = 0;
+        __syncthreads();
+        const size_t e = (size_t)myrank * kCk + i;
+        const uint32_t co = ck.off[e], cm = ck.m[e];
+        for (uint32_t k = threadIdx.x; k < cm; k += blockDim.x) {
+            const uint32_t q = ck.idx[co + k];
+            if (!in_clump[q] && owner[q] != myrank) s_lost = 1;
+        }
+        __syncthreads();
+        if (s_lost) {
+            first = i;
+            break;
+        }
+    }
+    if (threadIdx.x == 0) lost_ck[myrank] = first;
 }
 
 // Before a rerun pass: the particles of the clumps to be rerun become predictions (tent) of
@@ -2416,7 +2511,45 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
             PLAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rebind_loop, kRB, kRbSmem));
             rb_grid = std::max(1, nsm * std::max(1, per));
         }
-        uint64_t loop_launches = 0, suspensions = 0;
+        // Checkpoints of the clumps' runs (loop path): tables by key rank and a store for their
+        // member lists from what the arena has left; a rerun resumes from the last checkpoint
+        // before its first affected call (PLAN_REBIND_CHECKPOINTS=0: every rerun starts over)
+        uint32_t *d_ccall = nullptr, *d_dcall = nullptr, *d_dfirst = nullptr, *d_lostck = nullptr, *d_keep = nullptr;
+        Ckpt ck{};
+        {
+            const char *ck_env = std::getenv("PLAN_REBIND_CHECKPOINTS");
+            if (!use_rounds && !(ck_env && *ck_env == '0')) {
+                const size_t nr = (size_t)nlive + 1;
+                d_ccall = A.get<uint32_t>(nb);
+                d_dcall = A.get<uint32_t>(nb * kDeferSlots);
+                d_dfirst = A.get<uint32_t>(nb);
+                d_lostck = A.get<uint32_t>(nr);
+                d_keep = A.get<uint32_t>(nb);
+                ck.n = A.get<uint32_t>(nr);
+                ck.call = A.get<uint32_t>(nr * kCk);
+                ck.off = A.get<uint32_t>(nr * kCk);
+                ck.m = A.get<uint32_t>(nr * kCk);
+                ck.st = A.get<double>(nr * kCk * 8);
+                ck.top = A.get<uint32_t>(4);
+                if (A.failed) return kErrOutOfMemory;
+                const uint64_t used = (A.used + 255) & ~uint64_t(255), margin = 64ull * Tu + (256ull << 20);
+                const uint64_t ent = std::min<uint64_t>({A.cap > used + margin ? (A.cap - used - margin) / 12 : 0, 16ull * Tu, 0xfffffff0ull});
+                if (ent >= 4096) {
+                    ck.cap = (uint32_t)ent;
+                    ck.idx = A.get<uint32_t>(ent);
+                    ck.dist = A.get<double>(ent);
+                    if (A.failed) return kErrOutOfMemory;
+                    PLAN_CUDA(cudaMemsetAsync(ck.n, 0, nr * 4, s));
+                    PLAN_CUDA(cudaMemsetAsync(ck.top, 0, 4, s));
+                } else {
+                    ck = Ckpt{};
+                }
+                PLAN_CUDA(cudaMemsetAsync(d_ccall, 0, nb * 4, s));
+                PLAN_CUDA(cudaMemsetAsync(d_dcall, 0xff, nb * kDeferSlots * 4, s));
+                PLAN_CUDA(cudaMemsetAsync(d_dfirst, 0xff, nb * 4, s));
+            }
+        }
+        uint64_t loop_launches = 0, suspensions = 0, resumed = 0, calls_kept = 0;
         c.counters[24] = 0;  // members of the clumps each rebinding pass ran, summed over the passes
         // One pass of the device loop over `list` (key-rank order). Clumps that found the
         // member pool full stop with a consistent state; the pool is compacted and they
@@ -2481,6 +2614,10 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                 ra.err = c.d_err;
                 // a blocker's calls take longer on larger snapshots: the bound grows with them
                 ra.wait_limit = (uint32_t)std::min<uint64_t>(0xffffffffull, (uint64_t)kWaitLimit * std::max<uint64_t>(1, (Tu + (1u << 24) - 1) >> 24));
+                ra.ccall = d_ccall;
+                ra.dcall = d_dcall;
+                ra.dfirst = d_dfirst;
+                ra.ck = ck;
                 const unsigned grid = (unsigned)std::min<size_t>(todo.size(), (size_t)rb_grid);
                 double t_a = wall_ms();
                 if (c.kev[0]) cudaEventRecord(c.kev[0], s);
@@ -2654,6 +2791,7 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
         const bool front_only = front_env && *front_env == '1';
         std::vector<std::vector<uint32_t>> blockers(C);
         std::vector<unsigned long long> pred_hash(C, 0);
+        std::vector<uint32_t> keep_of(C, 0);  // per slot: checkpoints its next rerun keeps
         std::vector<uint32_t> active = live;
         for (uint32_t pass = 0; !active.empty(); ++pass) {
             if (pass > nlive + 2) return kErrDeviceLimit;
@@ -2707,17 +2845,30 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                 rc = st.up_list(live, st.d_list2);
                 if (rc) return rc;
                 k_rebind_verify<<<(unsigned)live.size(), 256, 0, s>>>(st.d_list2, (uint32_t)live.size(), ct, P, in_clump, owner, rank_of,
-                                                                      invalid, dset, dover, dmax);
+                                                                      invalid, dset, dover, dmax, ck, d_lostck);
                 c.launches++;
                 PLAN_CUDA(cudaGetLastError());
             }
             std::vector<uint8_t> inv, dov;
-            std::vector<uint32_t> dm, ds;
+            std::vector<uint32_t> dm, ds, hdc, hdf, hckn, hckc, hlost;
             rc = st.down(inv, invalid, C);
             if (!rc) rc = st.down(dm, dmax, C);
             if (!rc) rc = st.down(ds, dset, (size_t)C * kDeferSlots);
             if (!rc) rc = st.down(dov, dover, C);
+            if (!rc && ck.n) {
+                rc = st.down(hdc, d_dcall, (size_t)C * kDeferSlots);
+                if (!rc) rc = st.down(hdf, d_dfirst, C);
+                if (!rc) rc = st.down(hckn, ck.n, nlive);
+                if (!rc) rc = st.down(hckc, ck.call, (size_t)nlive * kCk);
+                if (!rc) rc = st.down(hlost, d_lostck, nlive);
+            }
             if (rc) return rc;
+            // checkpoints of rank r made after calls before j0
+            auto ck_before = [&](uint32_t r, uint32_t j0) -> uint32_t {
+                uint32_t k = 0;
+                while (k < hckn[r] && hckc[(size_t)r * kCk + k] < j0) ++k;
+                return k;
+            };
             // clumps of this pass whose members differ from the prediction the others used
             std::vector<uint8_t> changed(nlive + 1, 0);
             if (pass > 0) {
@@ -2739,25 +2890,39 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
             uint64_t why_inv = 0, why_dov = 0, why_rerun = 0, why_changed = 0;
             for (uint32_t r = 0; r < nlive; ++r) {
                 const uint32_t sl = live[r];
+                // checkpoints the rerun keeps: none before the first call it affects
+                uint32_t kp = ck.n ? hckn[r] : 0;
                 bool again = inv[sl] != 0;
                 why_inv += again;
-                if (!again && dov[sl]) {
-                    again = low != kNone && dm[sl] && dm[sl] - 1 >= low;
-                    why_dov += again;
-                } else if (!again) {
-                    for (int j = 0; j < kDeferSlots && !again; ++j) {
+                if (again && ck.n) kp = std::min(kp, hlost[r]);
+                if (dov[sl]) {  // the records overflowed: any deferral may be the first affected call
+                    const bool dep = low != kNone && dm[sl] && dm[sl] - 1 >= low;
+                    why_dov += dep && !again;
+                    if (dep && ck.n) kp = std::min(kp, ck_before(r, hdf[sl]));
+                    again = again || dep;
+                } else {
+                    for (int j = 0; j < kDeferSlots; ++j) {
                         const uint32_t d0 = ds[(size_t)sl * kDeferSlots + j];
                         if (d0 == kNone) continue;
                         // a partner that reruns; or one whose members differ from what this clump
                         // assumed (it saw a holding that could still change)
                         const uint32_t d = d0 & ~kDeferSpec;
                         const bool spec = use_rounds || (d0 & kDeferSpec) != 0;
-                        again = d < nlive && (rr[d] || (spec && changed[d]));
-                        why_rerun += again && rr[d];
-                        why_changed += again && !rr[d];
+                        const bool dep = d < nlive && (rr[d] || (spec && changed[d]));
+                        if (!dep) continue;
+                        if (!again) {
+                            why_rerun += rr[d];
+                            why_changed += !rr[d];
+                        }
+                        again = true;
+                        if (ck.n) kp = std::min(kp, ck_before(r, hdc[(size_t)sl * kDeferSlots + j]));
                     }
                 }
-                if (again) { rerun.push_back(sl); rr[r] = 1; }
+                if (again) {
+                    rerun.push_back(sl);
+                    rr[r] = 1;
+                    keep_of[sl] = kp;
+                }
                 if ((again || changed[r]) && low == kNone) low = r;
             }
             if (rerun.empty()) break;
@@ -2825,14 +2990,48 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                 }
             }
             reruns += rerun.size();
+            std::vector<uint32_t> keep(rerun.size(), 0);
+            uint32_t from_ck = 0;
+            for (size_t k = 0; k < rerun.size(); ++k) {
+                keep[k] = ck.n ? keep_of[rerun[k]] : 0;
+                if (keep[k]) {
+                    ++from_ck;
+                    calls_kept += hckc[(size_t)h_rank[rerun[k]] * kCk + keep[k] - 1];
+                }
+            }
+            resumed += from_ck;
+            trace.mark("  rerun starts (from the beginning, from a checkpoint)", (long long)(rerun.size() - from_ck), from_ck);
+            if (trace.fine_on && ck.n) {  // the largest reruns: where they resume, and why
+                std::vector<uint32_t> mnow;
+                rc = st.down(mnow, ct.mn, C);
+                if (rc) return rc;
+                std::vector<size_t> ord(rerun.size());
+                std::iota(ord.begin(), ord.end(), size_t(0));
+                std::sort(ord.begin(), ord.end(), [&](size_t x, size_t y) { return mnow[rerun[x]] > mnow[rerun[y]]; });
+                for (size_t q = 0; q < std::min<size_t>(6, ord.size()); ++q) {
+                    const uint32_t sl = rerun[ord[q]], r = h_rank[sl], kp = keep[ord[q]];
+                    std::fprintf(stderr, "[plan]     rerun rank %u members %u: checkpoints %u (last after call %u), keeps %u (to call %u); lost %d first-lost ck %u%s\n",
+                                 r, mnow[sl], hckn[r], hckn[r] ? hckc[(size_t)r * kCk + hckn[r] - 1] : 0, kp, kp ? hckc[(size_t)r * kCk + kp - 1] : 0,
+                                 (int)inv[sl], inv[sl] ? hlost[r] : 0, dov[sl] ? " (records overflowed)" : "");
+                    for (int j = 0; j < kDeferSlots; ++j) {
+                        const uint32_t d0 = ds[(size_t)sl * kDeferSlots + j];
+                        if (d0 == kNone) continue;
+                        const uint32_t d = d0 & ~kDeferSpec;
+                        std::fprintf(stderr, "[plan]       record rank %u%s call %u: %s\n", d, (d0 & kDeferSpec) ? " spec" : "", hdc[(size_t)sl * kDeferSlots + j],
+                                     d < nlive && rr[d] ? "reruns" : (d < nlive && changed[d]) ? "changed" : "-");
+                    }
+                }
+            }
             PLAN_CUDA(cudaMemcpyAsync(rerun_rank, rr.data(), nlive, cudaMemcpyHostToDevice, s));
             k_rebind_tentative<<<grid_for(Tu, 256), 256, 0, s>>>(Tu, owner, tent, rerun_rank);
             rc = st.maybe_compact();  // room for the restored segments
             if (rc) return rc;
             rc = st.up_list(rerun, st.d_list2);
             if (rc) return rc;
-            k_rebind_restore<<<(unsigned)rerun.size(), 256, 0, s>>>(st.d_list2, (uint32_t)rerun.size(), ct, P, bM, bh, bri, bro, br10, br2,
-                                                                    bc, bv, bo, bn, bidx, bdist, invalid, dmax, dset, dover, c.d_err);
+            if (ck.n) PLAN_CUDA(cudaMemcpyAsync(d_keep, keep.data(), keep.size() * 4, cudaMemcpyHostToDevice, s));
+            RestoreArgs ra{bM, bh, bri, bro, br10, br2, bc, bv, bo, bn, bidx, bdist, invalid, dover, d_distsq, d_needsort, dmax, dset,
+                           d_dcall, d_dfirst, d_ccall, owner, ck.n ? d_keep : nullptr, rank_of, in_clump, ck};
+            k_rebind_restore<<<(unsigned)rerun.size(), 256, 0, s>>>(st.d_list2, (uint32_t)rerun.size(), ct, P, ra, c.d_err);
             c.launches += 2;
             PLAN_CUDA(cudaGetLastError());
             active = rerun;
@@ -2842,6 +3041,8 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
         c.counters[14] = reruns;
         c.counters[12] = passes;
         c.counters[23] = suspensions;
+        c.counters[28] = resumed;     // reruns that resumed from a checkpoint
+        c.counters[29] = calls_kept;  // calls those resumptions did not redo
     }
     PLAN_CUDA(cudaStreamSynchronize(s));
     double tw3 = wall_ms();

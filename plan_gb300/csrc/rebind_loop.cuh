@@ -41,6 +41,7 @@ constexpr uint32_t kRbSmall = 4096;           // members sorted in shared memory
 constexpr uint32_t kWaitLimit = 1u << 25;     // bounded waits on blockers: sleeps of 1 us per 2^24 points
 constexpr uint32_t kCallLimit = 1u << 20;     // calls of one clump in one launch
 constexpr int kRbStats = 40;                  // counters per slot
+constexpr int kCk = 24;                       // checkpoints per clump and run
 // dynamic shared memory: the largest of the frontier, the small sort and the acceptance
 // tile (per candidate: FP64 position and velocity, index, FP32 form, taken flag)
 constexpr size_t kRbTileBytes = (size_t)kRB * (64 + 4 + sizeof(CandF) + 1);
@@ -50,6 +51,26 @@ static_assert(kRbFront * 14 <= kRbSmem, "frontier");
 static_assert(kRbTileBytes <= kRbSmem, "acceptance tile");
 static_assert(kRbSmall * 14 <= kRbSmem, "small sort");
 static_assert((256 + 256 * kRbWarps + 1) * 4 <= kRbSmem, "radix counters");
+
+// Checkpoints of the clumps' runs, by key rank: after the calls ck_after() selects, the
+// sorted member list (index, squared distance) and the state (M, centre, velocity, Hill
+// radius). A rerun resumes from the last checkpoint before its first affected call.
+struct Ckpt {
+    uint32_t *n;          // per rank: checkpoints kept
+    uint32_t *call, *off, *m;  // per rank x kCk: after which call, where in the store, members
+    double *st;           // per rank x kCk: M, cx, cy, cz, vx, vy, vz, hill
+    uint32_t *idx;        // the store (bump-allocated; a checkpoint that finds it full is not made)
+    double *dist;
+    uint32_t *top;
+    uint32_t cap;
+};
+
+// calls 1, 2, 3, 4, 6, 8, 12, 16, 24, 32, ...: a rerun redoes at most a third of the calls
+// before its first affected one
+__host__ __device__ inline bool ck_after(uint32_t j) {
+    if ((j & (j - 1)) == 0) return true;
+    return j % 3 == 0 && ((j / 3) & (j / 3 - 1)) == 0;
+}
 
 struct RbArgs {
     const uint32_t *list;  // clumps of this launch, in key-rank order
@@ -77,6 +98,9 @@ struct RbArgs {
     CP cp;
     unsigned *err;
     uint32_t wait_limit;   // sleeps a block waits for one blocker before it reports an error
+    uint32_t *ccall;       // per slot: calls of the clump's run done (persists across launches)
+    uint32_t *dcall, *dfirst;  // per deferral record / per slot: the earliest call that made it
+    Ckpt ck;               // ck.n null: no checkpoints
 };
 
 // per-point products for the member sums (src/tree.hpp:4436-4440: mass, pos * mass,
@@ -153,7 +177,7 @@ struct RbShared {
 // ------------------------------------------------------------------ one SearchBound call
 // Returns the number of accepted particles, or kNone when the member pool is full (nothing
 // changed).
-__device__ uint32_t rb_call(const RbArgs &a, uint32_t slot, uint32_t myrank, RbShared &sh, unsigned long long *stat) {
+__device__ uint32_t rb_call(const RbArgs &a, uint32_t slot, uint32_t myrank, RbShared &sh, unsigned long long *stat, uint32_t call) {
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     uint32_t *front = reinterpret_cast<uint32_t *>(sh.buf), *front2 = front + kRbFront, *fcnt = front2 + kRbFront;
     uint8_t *fcls = reinterpret_cast<uint8_t *>(fcnt + kRbFront), *fcls2 = fcls + kRbFront;
@@ -445,9 +469,10 @@ __device__ uint32_t rb_call(const RbArgs &a, uint32_t slot, uint32_t myrank, RbS
                 if (taken) atomicAdd(&sh.u[18], 1u);
             }
             if (ow != kNone && ow < myrank)
-                defer_add(a.dset, a.dover, a.dmax, slot, ow, *(volatile const uint8_t *)&a.finished[a.slot_of_rank[ow]] == 0);
+                defer_add(a.dset, a.dover, a.dmax, slot, ow, *(volatile const uint8_t *)&a.finished[a.slot_of_rank[ow]] == 0, a.dcall,
+                          a.dfirst, call);
             else if (tn != kNone && tn < myrank)
-                defer_add(a.dset, a.dover, a.dmax, slot, tn, true);
+                defer_add(a.dset, a.dover, a.dmax, slot, tn, true, a.dcall, a.dfirst, call);
             tpos[tid] = np;
             tvel[tid] = nv;
             tq[tid] = q;
@@ -892,6 +917,52 @@ __device__ bool rb_sort_particles(const RbArgs &a, uint32_t slot, RbShared &sh, 
     return ok;
 }
 
+// ------------------------------------------------------------------ checkpoints
+__device__ uint32_t ck_try_alloc(const Ckpt &ck, uint32_t n) {
+    uint32_t cur = *(volatile uint32_t *)ck.top;
+    for (int it = 0; it < (1 << 22); ++it) {
+        if ((uint64_t)cur + n > ck.cap) return kNone;
+        const uint32_t prev = atomicCAS(ck.top, cur, cur + n);
+        if (prev == cur) return cur;
+        cur = prev;
+    }
+    return kNone;
+}
+
+// the clump's state after call j (its members just sorted): a checkpoint, if there is room
+__device__ void rb_checkpoint(const RbArgs &a, uint32_t slot, uint32_t rank, uint32_t j, RbShared &sh) {
+    const int tid = threadIdx.x;
+    uint32_t &s_off = sh.u[19];
+    const uint32_t o = a.ct.moff[slot], m = a.ct.mn[slot];
+    if (tid == 0) {
+        s_off = kNone;
+        if (a.ck.n[rank] < (uint32_t)kCk) s_off = ck_try_alloc(a.ck, m);
+    }
+    __syncthreads();
+    const uint32_t off = s_off;
+    if (off != kNone) {
+        for (uint32_t k = tid; k < m; k += kRB) {
+            a.ck.idx[off + k] = a.P.idx[o + k];
+            a.ck.dist[off + k] = a.P.dist[o + k];
+        }
+        if (tid == 0) {
+            const uint32_t n = a.ck.n[rank];
+            const size_t e = (size_t)rank * kCk + n;
+            const double4_32a c = a.ct.com[slot], v = a.ct.vcom[slot];
+            double *q = a.ck.st + e * 8;
+            q[0] = a.ct.M[slot];
+            q[1] = c.x; q[2] = c.y; q[3] = c.z;
+            q[4] = v.x; q[5] = v.y; q[6] = v.z;
+            q[7] = a.ct.hill[slot];
+            a.ck.call[e] = j;
+            a.ck.off[e] = off;
+            a.ck.m[e] = m;
+            a.ck.n[rank] = n + 1;
+        }
+    }
+    __syncthreads();
+}
+
 // ------------------------------------------------------------------ the persistent loop
 __global__ void __launch_bounds__(kRB, 1) k_rebind_loop(RbArgs a) {
     extern __shared__ __align__(16) unsigned char rb_dyn[];
@@ -925,6 +996,10 @@ __global__ void __launch_bounds__(kRB, 1) k_rebind_loop(RbArgs a) {
         __syncthreads();
         const uint32_t myrank = a.rank_of[slot];
         unsigned long long *stat = a.stats ? a.stats + kRbStats * (size_t)slot : nullptr;
+        if (tid == 0) s_item = a.ccall[slot];
+        __syncthreads();
+        uint32_t done = s_item;  // calls of this clump's run so far
+        __syncthreads();
         bool suspend = false;
         if (a.needsort[slot]) suspend = !rb_sort_particles(a, slot, sh, stat);
         for (uint32_t call = 0; !suspend; ++call) {
@@ -932,13 +1007,17 @@ __global__ void __launch_bounds__(kRB, 1) k_rebind_loop(RbArgs a) {
                 if (tid == 0) atomicOr(a.err, (unsigned)kDevErrLoopLimit);
                 break;
             }
-            const uint32_t nacc = rb_call(a, slot, myrank, sh, stat);
+            const uint32_t j = done + 1;
+            const uint32_t nacc = rb_call(a, slot, myrank, sh, stat, j);
             if (nacc == kNone) {
                 suspend = true;
                 break;
             }
+            done = j;
+            if (tid == 0) a.ccall[slot] = j;
             if (nacc == 0) break;  // no growth: the Hill radius of the unchanged mass stays
             if (!rb_sort_particles(a, slot, sh, stat)) suspend = true;
+            else if (a.ck.n && ck_after(j)) rb_checkpoint(a, slot, myrank, j, sh);
         }
         if (!suspend && a.distsq[slot]) {  // the distances of the last sort
             const uint32_t o = a.ct.moff[slot], m = a.ct.mn[slot];
