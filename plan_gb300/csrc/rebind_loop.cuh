@@ -293,6 +293,8 @@ __device__ uint32_t rb_call(const RbArgs &a, uint32_t slot, uint32_t myrank, RbS
             }
             q = a.E[front2[lo] + (tt - fcnt[lo])];
             keep = fcls[lo] == 1 || in_ball(t, a.ft, ball, q);
+            // this clump's own claims are its members: the acceptance would only skip them
+            if (keep && __ldcg(&a.owner[q]) == myrank) keep = false;
         }
         uint32_t r;
         const uint32_t tot = rb_block_rank(keep, r, sh.warp_tot);
