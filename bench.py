@@ -534,7 +534,8 @@ def run_serve(args) -> None:
             "config": {"workload": f"{len(reqs)} requests of the workload's mixture, N log-uniform in [2^16, 2^{args.serve_max_log2}], "
                                    f"Poisson arrivals at {args.serve_rate}/s", "workers": args.serve_workers, "particles": n_tot},
             "served": {"snapshots_per_s": len(reqs) / served_s, "particles_per_s": n_tot / served_s,
-                       "latency_ms": latency_stats(served_lat), "peak_held_bytes": st["peak_held_bytes"], "releases": st["releases"]},
+                       "latency_ms": latency_stats(served_lat), "peak_held_bytes": st["peak_held_bytes"], "releases": st["releases"],
+                       "busy_ms": st["busy_ms"], "two_or_more_running_ms": st["overlap_ms"]},
             "plain": {"snapshots_per_s": len(reqs) / plain_s, "particles_per_s": n_tot / plain_s, "latency_ms": latency_stats(plain_lat)},
             "identical_catalogues": same, "clocks": clk}
     print(json.dumps(line), flush=True)

@@ -202,6 +202,10 @@ int plan_poll(plan_server *srv, uint64_t request, int wait, plan_catalogue **out
 const char *plan_server_error(const plan_server *srv);
 /* Largest sum of worker holds seen against the budget, and how many holds were given back. */
 int plan_server_stats(const plan_server *srv, uint64_t *peak_held_bytes, uint64_t *releases);
+/* Over the requests run so far, each from its start on a worker to its end: the time at least
+ * one ran (busy_ms) and the time two or more ran at once on their workers' streams
+ * (overlap_ms). No reference counterpart: it shows the workers' work overlapping. */
+int plan_server_overlap(const plan_server *srv, double *busy_ms, double *overlap_ms);
 
 /* ---------------------------------------------------------------- inspection
  * Stage arrays of the last snapshot, for parity tests and profiling. */

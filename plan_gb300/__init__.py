@@ -119,6 +119,7 @@ def lib() -> C.CDLL:
             "plan_poll": (i32, [vp, u64, i32, C.POINTER(vp), C.POINTER(C.c_double)]),
             "plan_server_error": (C.c_char_p, [vp]),
             "plan_server_stats": (i32, [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+            "plan_server_overlap": (i32, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
             "plan_catalogue_basic_results": (i32, [vp, C.POINTER(Params), i32, C.c_char_p, C.c_size_t]),
             "plan_stage_count": (u64, [vp, i32]),
             "plan_stage_copy": (i32, [vp, i32, vp, C.c_size_t]),
@@ -147,7 +148,7 @@ EXPORTED = [
     "plan_build_tree", "plan_find_planetesimals", "plan_find_clumps", "plan_catalogue_free", "plan_catalogue_count",
     "plan_catalogue_get", "plan_catalogue_summary", "plan_catalogue_write_peaks", "plan_catalogue_write_parlists",
     "plan_catalogue_basic_results", "plan_ctx_release", "plan_group_energies", "plan_density_vs_scale", "plan_server_create", "plan_server_destroy", "plan_submit", "plan_poll",
-    "plan_server_error", "plan_server_stats",
+    "plan_server_error", "plan_server_stats", "plan_server_overlap",
     "plan_stage_count", "plan_stage_copy", "plan_knn", "plan_morton_order", "plan_morton_order_noalloc", "plan_stage_times", "plan_kernel_launches", "plan_counters",
     "plan_synth_default_spec", "plan_synth_records", "plan_synth_write_lis", "plan_synth_four_pi_G_for_mean",
 ]
@@ -445,7 +446,10 @@ class Server:
     def stats(self) -> dict:
         peak, rel = C.c_uint64(), C.c_uint64()
         lib().plan_server_stats(self._h, C.byref(peak), C.byref(rel))
-        return {"peak_held_bytes": int(peak.value), "releases": int(rel.value)}
+        busy, both = C.c_double(), C.c_double()
+        lib().plan_server_overlap(self._h, C.byref(busy), C.byref(both))
+        return {"peak_held_bytes": int(peak.value), "releases": int(rel.value), "busy_ms": float(busy.value),
+                "overlap_ms": float(both.value)}
 
     def close(self):
         if self._h:

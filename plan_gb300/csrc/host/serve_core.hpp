@@ -11,6 +11,7 @@
 // the room (the release runs before that request starts, so the budget holds on the device).
 #pragma once
 
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <cstdint>
@@ -121,6 +122,27 @@ class ServeQueue {
         std::unique_lock<std::mutex> lk(mu_);
         return releases_;
     }
+    // Over the requests run so far, from each one's start on its worker to its end: the time
+    // at least one ran (busy_ms) and the time two or more ran at once (overlap_ms).
+    void overlap(double &busy_ms, double &overlap_ms) const {
+        std::vector<std::pair<std::chrono::steady_clock::time_point, int>> ev;
+        {
+            std::unique_lock<std::mutex> lk(mu_);
+            for (const auto &sp : spans_) {
+                ev.emplace_back(sp.first, +1);
+                ev.emplace_back(sp.second, -1);
+            }
+        }
+        std::sort(ev.begin(), ev.end(), [](const auto &a, const auto &b) { return a.first < b.first || (a.first == b.first && a.second < b.second); });
+        busy_ms = overlap_ms = 0;
+        int running = 0;
+        for (size_t k = 0; k + 1 < ev.size(); ++k) {
+            running += ev[k].second;
+            const double dt = std::chrono::duration<double, std::milli>(ev[k + 1].first - ev[k].first).count();
+            if (running >= 1) busy_ms += dt;
+            if (running >= 2) overlap_ms += dt;
+        }
+    }
     int workers() const { return (int)held_.size(); }
     // once true, stays true: submit refuses everything from then on
     bool stopping() const {
@@ -218,6 +240,7 @@ class ServeQueue {
             const int rc = init_rc ? init_rc : run_(w, *r);
             r->t_done = std::chrono::steady_clock::now();
             lk.lock();
+            spans_.emplace_back(r->t_start, r->t_done);
             r->status = rc < 0 ? 1000 : rc;
             assigned_[w] = nullptr;
             busy_[w] = 0;
@@ -235,6 +258,7 @@ class ServeQueue {
     std::vector<uint64_t> held_;
     std::vector<uint8_t> busy_, release_pending_;
     std::vector<std::shared_ptr<ServeRequest>> assigned_;
+    std::vector<std::pair<std::chrono::steady_clock::time_point, std::chrono::steady_clock::time_point>> spans_;
     std::vector<std::thread> threads_;
     uint64_t budget_, next_id_ = 0, peak_held_ = 0, releases_ = 0, started_ = 0;
     uint32_t max_bypass_;

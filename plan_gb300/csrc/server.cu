@@ -153,4 +153,13 @@ int plan_server_stats(const plan_server *srv, uint64_t *peak_held_bytes, uint64_
     return plan::kOk;
 }
 
+int plan_server_overlap(const plan_server *srv, double *busy_ms, double *overlap_ms) {
+    if (!srv) return plan::kErrArgument;
+    double b = 0, o = 0;
+    srv->q->overlap(b, o);
+    if (busy_ms) *busy_ms = b;
+    if (overlap_ms) *overlap_ms = o;
+    return plan::kOk;
+}
+
 }  // extern "C"

@@ -89,9 +89,12 @@ static int run_case(int workers, uint64_t budget, uint32_t max_bypass, int nreq,
         }
     ServeRequest r;
     if (q.take(999999, false, r) != -1) ++wrong;
+    double busy = 0, both = 0;
+    q.overlap(busy, both);
     q.shutdown();
-    std::printf("%d %llu %llu %ld %ld %ld %ld %d %d %d %llu\n", workers, (unsigned long long)budget, (unsigned long long)ck.worst, ck.bad,
-                done, wrong, bypass_bad + order_bad, rejected.load(), inits.load(), finis.load(), (unsigned long long)q.releases());
+    std::printf("%d %llu %llu %ld %ld %ld %ld %d %d %d %llu %lld %lld\n", workers, (unsigned long long)budget, (unsigned long long)ck.worst, ck.bad,
+                done, wrong, bypass_bad + order_bad, rejected.load(), inits.load(), finis.load(), (unsigned long long)q.releases(),
+                (long long)(busy * 1000), (long long)(both * 1000));
     return 0;
 }
 
@@ -116,10 +119,14 @@ def test_serving_admission(tmp_path):
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True, timeout=120).stdout.split("\n")
     rows = [list(map(int, ln.split())) for ln in out if ln.strip()]
     assert len(rows) == 5
-    for workers, budget, worst, over, done, wrong, order, rejected, inits, finis, releases in rows:
+    for workers, budget, worst, over, done, wrong, order, rejected, inits, finis, releases, busy_us, both_us in rows:
+        assert busy_us > 0 and 0 <= both_us <= busy_us  # run spans: some time busy, overlap within it
+        if workers == 1:
+            assert both_us == 0                       # one worker never runs two at once
         assert over == 0 and worst <= budget          # the holds never exceed the budget
         assert wrong == 0 and done > 0                # every request ran once, with its own result
         assert order == 0                             # bypass bound and strict order kept
         assert rejected == 1                          # a snapshot larger than the budget is refused
         assert inits == workers and finis == workers  # one context per worker, torn down at the end
     assert any(r[10] > 0 for r in rows)               # idle workers gave buffers back when needed
+    assert rows[3][12] > 0                            # eight workers, everything fits: requests overlap
