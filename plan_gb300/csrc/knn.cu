@@ -275,14 +275,21 @@ __global__ void __launch_bounds__(128) k_density_f(KTree t, FTree f, uint32_t n,
     extern __shared__ unsigned char smem[];
     float *sk = reinterpret_cast<float *>(smem);
     uint32_t *si = reinterpret_cast<uint32_t *>(sk + CAP * blockDim.x);
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool act = i < n;  // every lane reaches the reconvergence point below
     FHeap fh{sk + threadIdx.x, si + threadIdx.x, (int)blockDim.x};
     double d64[CAP];
     uint32_t i64[CAP];
-    double4_32a q = t.pos[i];
-    double r = knn_first_radius(t, q.x, q.y, q.z, t.leaf_of[i], k, err);
-    int got = knn_query_f32(t, f, i, q.x, q.y, q.z, r, k, CAP, fh, d64, i64, err);
+    double4_32a q = make_double4_32a(0, 0, 0, 0);
+    int z = -1;
+    if (act) {
+        q = t.pos[i];
+        const double r = knn_first_radius(t, q.x, q.y, q.z, t.leaf_of[i], k, err);
+        z = knn_collect_f32(t, f, i, r, k, CAP, fh, err);
+    }
+    __syncwarp();  // the walks diverge; the FP64 part runs with the whole warp
+    const int got = z >= 0 ? knn_exact_f32(t, q.x, q.y, q.z, k, z, fh, d64, i64) : -1;
+    if (!act) return;
     if (got < 0) {
         redo[atomicAdd(nredo, 1u)] = i;
         return;
@@ -297,17 +304,25 @@ __global__ void __launch_bounds__(128) k_densest_f(KTree t, FTree f, uint32_t n,
     extern __shared__ unsigned char smem[];
     float *sk = reinterpret_cast<float *>(smem);
     uint32_t *si = reinterpret_cast<uint32_t *>(sk + CAP * blockDim.x);
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    double di = dens[i];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool act = i < n;  // every lane reaches the reconvergence point below
+    const double di = act ? dens[i] : 0.0;
     uint32_t best = i;
-    if (di >= threshold) {  // src/tree.hpp:3719-3735
-        FHeap fh{sk + threadIdx.x, si + threadIdx.x, (int)blockDim.x};
-        double d64[CAP];
-        uint32_t i64[CAP];
-        double4_32a q = t.pos[i];
-        double r = knn_first_radius(t, q.x, q.y, q.z, t.leaf_of[i], k, err);
-        int got = knn_query_f32(t, f, i, q.x, q.y, q.z, r, k, CAP, fh, d64, i64, err);
+    const bool walk = act && di >= threshold;  // src/tree.hpp:3719-3735
+    FHeap fh{sk + threadIdx.x, si + threadIdx.x, (int)blockDim.x};
+    double d64[CAP];
+    uint32_t i64[CAP];
+    double4_32a q = make_double4_32a(0, 0, 0, 0);
+    int z = -1;
+    if (walk) {
+        q = t.pos[i];
+        const double r = knn_first_radius(t, q.x, q.y, q.z, t.leaf_of[i], k, err);
+        z = knn_collect_f32(t, f, i, r, k, CAP, fh, err);
+    }
+    __syncwarp();  // the walks diverge; the FP64 part runs with the whole warp
+    const int got = z >= 0 ? knn_exact_f32(t, q.x, q.y, q.z, k, z, fh, d64, i64) : -1;
+    if (!act) return;
+    if (walk) {
         if (got < 0) {
             redo[atomicAdd(nredo, 1u)] = i;
             return;

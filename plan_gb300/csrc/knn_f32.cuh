@@ -175,13 +175,15 @@ __device__ __forceinline__ float f_dr2(const float4 qh, const float4 ql, const f
 __device__ __forceinline__ float f_hi(float v) { return v * (1.f + kRel) + 1e-24f; }
 __device__ __forceinline__ float f_lo(float v) { return v * (1.f - kRel) - 1e-24f; }
 
-// Exact k-nearest of the reference for one query through the FP32 filter. On success fills
-// d64/i64 (ascending exact dr2, the reference's k-set) and returns k; returns -1 when the
-// query must take the exact FP64 path.
+// Exact k-nearest of the reference for one query through the FP32 filter, in two parts.
+// knn_collect_f32 walks the tree in FP32 and leaves the candidates in ascending FP32 order in
+// the heap slab; it returns how many of them could belong to the k nearest (z), or -1 when
+// the query must take the exact FP64 path. knn_exact_f32 then takes their exact FP64
+// distances. The callers let the warp reconverge between the two (the walks of a warp's
+// queries diverge; the FP64 part, whose instructions cost the same for one lane as for 32,
+// then runs for all lanes at once).
 // Slab layout per thread: cap = k + slack entries of (float key, u32 idx) and of (double, u32).
-__device__ inline int knn_query_f32(const KTree &t, const FTree &f, uint32_t qi, double qx, double qy, double qz, double r, uint32_t k,
-                                    int cap, FHeap &fh, double *d64, uint32_t *i64, unsigned *err) {
-    const int dstride = 1;
+__device__ inline int knn_collect_f32(const KTree &t, const FTree &f, uint32_t qi, double r, uint32_t k, int cap, FHeap &fh, unsigned *err) {
     const float4 qh = f.phi[qi], ql = f.plo[qi];
     // radius doubling with count-only passes
     for (int it = 0; it < 200; ++it) {
@@ -218,6 +220,14 @@ __device__ inline int knn_query_f32(const KTree &t, const FTree &f, uint32_t qi,
     if ((int)visited > size && !(f_lo(fh.kget(size - 1)) > thr)) return -1;  // buffer might miss candidates
     int z = 0;
     while (z < size && !(f_lo(fh.kget(z)) > thr)) ++z;
+    return z;
+}
+
+// The second part: fills d64/i64 (ascending exact dr2, the reference's k-set) from the z
+// candidates and returns k, or -1 on a tie the library heap order decides.
+__device__ inline int knn_exact_f32(const KTree &t, double qx, double qy, double qz, uint32_t k, int z, const FHeap &fh, double *d64,
+                                    uint32_t *i64) {
+    const int dstride = 1;
     // exact FP64 distances for every possible member, insertion-sorted by (dr2, index)
     for (int j = 0; j < z; ++j) {
         uint32_t p = fh.ix[j * fh.stride];
