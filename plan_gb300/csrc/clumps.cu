@@ -2511,18 +2511,27 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
             PLAN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_rebind_loop, kRB, kRbSmem));
             rb_grid = std::max(1, nsm * std::max(1, per));
         }
-        // Checkpoints of the clumps' runs (loop path): tables by key rank and a store for their
-        // member lists from what the arena has left; a rerun resumes from the last checkpoint
-        // before its first affected call (PLAN_REBIND_CHECKPOINTS=0: every rerun starts over)
+        // Checkpoints of the clumps' runs (loop path, PLAN_REBIND_CHECKPOINTS=1): tables by key
+        // rank and a store for their member lists from what the arena has left; a rerun then
+        // resumes from the last checkpoint before its first affected call. Off by default: the
+        // kept calls may hold particles that an earlier clump rerunning in the same pass takes
+        // in its new run, which costs another pass (measured: 1M snapshot 2 -> 3 passes, 16.7M
+        // no better), where a rerun from the start would have waited for that clump.
         uint32_t *d_ccall = nullptr, *d_dcall = nullptr, *d_dfirst = nullptr, *d_lostck = nullptr, *d_keep = nullptr;
         Ckpt ck{};
+        if (!use_rounds) {  // the calls of each run and of each deferral record: with or without checkpoints
+            d_ccall = A.get<uint32_t>(nb);
+            d_dcall = A.get<uint32_t>(nb * kDeferSlots);
+            d_dfirst = A.get<uint32_t>(nb);
+            if (A.failed) return kErrOutOfMemory;
+            PLAN_CUDA(cudaMemsetAsync(d_ccall, 0, nb * 4, s));
+            PLAN_CUDA(cudaMemsetAsync(d_dcall, 0xff, nb * kDeferSlots * 4, s));
+            PLAN_CUDA(cudaMemsetAsync(d_dfirst, 0xff, nb * 4, s));
+        }
         {
             const char *ck_env = std::getenv("PLAN_REBIND_CHECKPOINTS");
-            if (!use_rounds && !(ck_env && *ck_env == '0')) {
+            if (!use_rounds && ck_env && *ck_env == '1') {
                 const size_t nr = (size_t)nlive + 1;
-                d_ccall = A.get<uint32_t>(nb);
-                d_dcall = A.get<uint32_t>(nb * kDeferSlots);
-                d_dfirst = A.get<uint32_t>(nb);
                 d_lostck = A.get<uint32_t>(nr);
                 d_keep = A.get<uint32_t>(nb);
                 ck.n = A.get<uint32_t>(nr);
@@ -2544,9 +2553,6 @@ int find_planetesimals(Context &c, plan_params &p, cudaStream_t s, plan_catalogu
                 } else {
                     ck = Ckpt{};
                 }
-                PLAN_CUDA(cudaMemsetAsync(d_ccall, 0, nb * 4, s));
-                PLAN_CUDA(cudaMemsetAsync(d_dcall, 0xff, nb * kDeferSlots * 4, s));
-                PLAN_CUDA(cudaMemsetAsync(d_dfirst, 0xff, nb * 4, s));
             }
         }
         uint64_t loop_launches = 0, suspensions = 0, resumed = 0, calls_kept = 0;

@@ -998,7 +998,7 @@ __global__ void __launch_bounds__(kRB, 1) k_rebind_loop(RbArgs a) {
         __syncthreads();
         const uint32_t myrank = a.rank_of[slot];
         unsigned long long *stat = a.stats ? a.stats + kRbStats * (size_t)slot : nullptr;
-        if (tid == 0) s_item = a.ccall[slot];
+        if (tid == 0) s_item = a.ccall ? a.ccall[slot] : 0u;
         __syncthreads();
         uint32_t done = s_item;  // calls of this clump's run so far
         __syncthreads();
@@ -1016,7 +1016,7 @@ __global__ void __launch_bounds__(kRB, 1) k_rebind_loop(RbArgs a) {
                 break;
             }
             done = j;
-            if (tid == 0) a.ccall[slot] = j;
+            if (tid == 0 && a.ccall) a.ccall[slot] = j;
             if (nacc == 0) break;  // no growth: the Hill radius of the unchanged mass stays
             if (!rb_sort_particles(a, slot, sh, stat)) suspend = true;
             else if (a.ck.n && ck_after(j)) rb_checkpoint(a, slot, myrank, j, sh);
