@@ -44,38 +44,60 @@ extern "C" int tiles_cover(uint64_t T) {
     return 1;
 }
 
-// the GPU's pass over one group, replayed: every tile, 128 row threads, FP64 tree reduction
-extern "C" double pair_sum_host(const float *pos3, const float *mass, uint64_t n, uint64_t *zeros_out) {
-    const uint64_t T = (n + kPairTile - 1) / kPairTile;
+// the GPU's pass over one group, replayed: every w x w tile, w row threads, FP64 tree
+// reduction per tile into its own slot, then the slots added in tile order
+extern "C" double pair_sum_host_w(const float *pos3, const float *mass, uint64_t n, int w, uint64_t *zeros_out) {
+    const uint64_t T = (n + w - 1) / w;
     double total = 0.0;
     uint64_t zeros = 0;
-    std::vector<PairParticle> col(kPairTile);
+    std::vector<PairParticle> col(w);
+    std::vector<double> red(w);
     for (uint64_t l = 0; l < T * (T + 1) / 2; ++l) {
         uint64_t ti, tj;
         tile_of(l, T, ti, tj);
-        const uint64_t c0 = tj * kPairTile;
-        for (int t = 0; t < kPairTile; ++t)
+        const uint64_t c0 = tj * w;
+        for (int t = 0; t < w; ++t)
             if (c0 + t < n) col[t] = PairParticle{pos3[3 * (c0 + t)], pos3[3 * (c0 + t) + 1], pos3[3 * (c0 + t) + 2], mass[c0 + t]};
-        double red[kPairTile];
-        for (int t = 0; t < kPairTile; ++t) {
-            const uint64_t r = ti * kPairTile + t;
+        for (int t = 0; t < w; ++t) {
+            const uint64_t r = ti * w + t;
             float s = 0.f, c = 0.f;
             uint32_t z = 0;
             double mrow = 0;
             if (r < n) {
-                const uint32_t cn = (uint32_t)(n - c0 < (uint64_t)kPairTile ? n - c0 : (uint64_t)kPairTile);
+                const uint32_t cn = (uint32_t)(n - c0 < (uint64_t)w ? n - c0 : (uint64_t)w);
                 pair_row_sum(PairParticle{pos3[3 * r], pos3[3 * r + 1], pos3[3 * r + 2], mass[r]}, col.data(), cn, ti == tj ? t : -1, s, c, z);
                 mrow = mass[r];
             }
             red[t] = mrow * ((double)s + (double)c);
             zeros += z;
         }
-        for (int h = kPairTile / 2; h > 0; h >>= 1)
+        for (int h = w / 2; h > 0; h >>= 1)
             for (int t = 0; t < h; ++t) red[t] += red[t + h];
         total += red[0];
     }
     *zeros_out = zeros;
     return total;
+}
+
+extern "C" double pair_sum_host(const float *pos3, const float *mass, uint64_t n, uint64_t *zeros_out) {
+    return pair_sum_host_w(pos3, mass, n, kPairTile, zeros_out);
+}
+
+extern "C" int energy_class_host(uint64_t n) { return energy_class(n); }
+
+extern "C" int energy_table_ok() {
+    for (int k = 0; k < kEnergyClasses; ++k)
+        if (!energy_tile_ok(kEnergyTile[k])) return 0;
+    for (int k = 0; k + 1 < kEnergyClasses - 1; ++k)
+        if (kEnergyClassBound[k] >= kEnergyClassBound[k + 1]) return 0;
+    return 1;
+}
+
+extern "C" int pair_items_tile_host(const uint64_t *offsets, uint32_t ngroups, uint32_t tile, uint64_t *out) {
+    std::vector<uint64_t> v;
+    const int rc = pair_items(offsets, ngroups, v, tile);
+    for (size_t i = 0; i < v.size(); ++i) out[i] = v[i];
+    return rc;
 }
 """
 
@@ -94,6 +116,12 @@ def shim(tmp_path_factory):
     L.tiles_cover.argtypes = [C.c_uint64]
     L.pair_sum_host.restype = C.c_double
     L.pair_sum_host.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]
+    L.pair_sum_host_w.restype = C.c_double
+    L.pair_sum_host_w.argtypes = [C.c_void_p, C.c_void_p, C.c_uint64, C.c_int, C.POINTER(C.c_uint64)]
+    L.energy_class_host.restype = C.c_int
+    L.energy_class_host.argtypes = [C.c_uint64]
+    L.pair_items_tile_host.restype = C.c_int
+    L.pair_items_tile_host.argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p]
     return L
 
 
@@ -163,3 +191,29 @@ def test_pair_items_over_groups(shim):
     assert out.tolist() == [0, 0, 1, 2, 5, 20]  # n = 0, 1, 128, 171, 640: T = 0, 1, 1, 2, 5
     bad = np.array([0, 10, 5], dtype=np.uint64)
     assert shim.pair_items_host(bad.ctypes.data, 2, out.ctypes.data) == -1
+
+
+@pytest.mark.parametrize("w", [32, 64, 128, 256])
+@pytest.mark.parametrize("n", [2, 33, 300, 1000])
+def test_tiled_pass_every_tile_width(w, n, shim):
+    """Every width the pass is built for (one per size class) covers each pair once and stays
+    within the stated 1e-6 of the FP64 direct sum."""
+    pos, vel, mass = plummer_group(n, 7 * n + w)
+    z = C.c_uint64()
+    got = shim.pair_sum_host_w(pos.ctypes.data, mass.ctypes.data, n, w, C.byref(z))
+    want = fp64_potential_sum(pos, mass)
+    assert z.value == 0
+    assert abs(got - want) <= 1e-6 * abs(want), (w, n, got, want)
+
+
+def test_size_classes_and_their_queues(shim):
+    """Groups of n < 64, < 512, < 8192 and larger particles are classes 0-3; the measured
+    table holds widths the pass is built for; each class's queue counts its groups' tiles at
+    its own width."""
+    assert shim.energy_table_ok() == 1
+    got = [shim.energy_class_host(n) for n in (0, 1, 63, 64, 511, 512, 8191, 8192, 10 ** 7)]
+    assert got == [0, 0, 0, 1, 1, 2, 2, 3, 3]
+    off = np.array([0, 31, 64, 97, 97 + 256], dtype=np.uint64)  # n = 31, 33, 33, 256
+    out = np.zeros(len(off), dtype=np.uint64)
+    assert shim.pair_items_tile_host(off.ctypes.data, len(off) - 1, 32, out.ctypes.data) == 0
+    assert out.tolist() == [0, 1, 4, 7, 43]  # T = 1, 2, 2, 8 tiles per side at width 32
