@@ -708,7 +708,19 @@ __global__ void k_rekey(uint32_t C, CT ct, const uint32_t *order, uint32_t n, Po
     *nfail += fails;
 }
 
-// RemoveUnboundParticles (src/tree.hpp:4615-4674) for a list of clumps, one block each.
+// RN(num / den) given y = RN(1 / den): q0 = RN(num y), then Markstein's correction
+// RN(q0 + (num - q0 den) y) with two FMAs is the correctly rounded quotient (the identity
+// tests/test_div_host.py checks against IEEE division); a zero numerator is returned as it
+// is, which is the quotient for den > 0. Several quotients by one divisor then cost one
+// reciprocal and two FMAs each instead of a division each.
+__device__ __forceinline__ double div_by_rcp(double num, double den, double y) {
+    if (num == 0.0) return num;
+    const double q0 = num * y;
+    return fma(fma(-q0, den, num), y, q0);
+}
+
+// RemoveUnboundParticles (src/tree.hpp:4615-4674) for a list of clumps, one block each. The
+// six quotients by the remaining mass share one correctly rounded reciprocal (div_by_rcp).
 __global__ void __launch_bounds__(256) k_unbind(const uint32_t *list, CT ct, Pool P, const double4_32a *pos, const double4_32a *vel, CP cp) {
     __shared__ double sM, scx, scy, scz, svx, svy, svz;
     __shared__ int s_best;
@@ -735,9 +747,12 @@ __global__ void __launch_bounds__(256) k_unbind(const uint32_t *list, CT ct, Poo
             uint32_t pi = P.idx[o + j];
             double4_32a p = pos[pi], v = vel[pi];
             double M = sM;
-            Mr = M - p.w;
-            double cx = (scx * M - p.x * p.w) / Mr, cy = (scy * M - p.y * p.w) / Mr, cz = (scz * M - p.z * p.w) / Mr;
-            double vx = (svx * M - v.x * p.w) / Mr, vy = (svy * M - v.y * p.w) / Mr, vz = (svz * M - v.z * p.w) / Mr;
+            Mr = M - p.w;  // > 0: at least two members remain
+            const double y = __drcp_rn(Mr);
+            double cx = div_by_rcp(scx * M - p.x * p.w, Mr, y), cy = div_by_rcp(scy * M - p.y * p.w, Mr, y),
+                   cz = div_by_rcp(scz * M - p.z * p.w, Mr, y);
+            double vx = div_by_rcp(svx * M - v.x * p.w, Mr, y), vy = div_by_rcp(svy * M - v.y * p.w, Mr, y),
+                   vz = div_by_rcp(svz * M - v.z * p.w, Mr, y);
             double dx = cx - p.x;
             double ex = (vx - 0.0 * dx) - v.x, ey = (vy - cp.shear * dx) - v.y, ez = (vz - 0.0 * dx) - v.z;
             double e = +0.5 / M * norm2_3(ex, ey, ez) - cp.G / norm3(cx - p.x, cy - p.y, cz - p.z);
@@ -756,8 +771,11 @@ __global__ void __launch_bounds__(256) k_unbind(const uint32_t *list, CT ct, Poo
             double4_32a p = pos[pi], v = vel[pi];
             double M = sM;
             double Mr2 = M - p.w;
-            scx = (scx * M - p.x * p.w) / Mr2; scy = (scy * M - p.y * p.w) / Mr2; scz = (scz * M - p.z * p.w) / Mr2;
-            svx = (svx * M - v.x * p.w) / Mr2; svy = (svy * M - v.y * p.w) / Mr2; svz = (svz * M - v.z * p.w) / Mr2;
+            const double y2 = __drcp_rn(Mr2);
+            scx = div_by_rcp(scx * M - p.x * p.w, Mr2, y2); scy = div_by_rcp(scy * M - p.y * p.w, Mr2, y2);
+            scz = div_by_rcp(scz * M - p.z * p.w, Mr2, y2);
+            svx = div_by_rcp(svx * M - v.x * p.w, Mr2, y2); svy = div_by_rcp(svy * M - v.y * p.w, Mr2, y2);
+            svz = div_by_rcp(svz * M - v.z * p.w, Mr2, y2);
             sM = Mr2;
             // swap with the back and pop (src/tree.hpp:4660-4663)
             uint32_t bk = s_back;
