@@ -55,8 +55,9 @@ DENSITY_BYTES_PER_POINT = 12 + 8 + 4 * KNN + 4
 # clumps it ran
 REBIND_BYTES_PER_MEMBER = 28
 # dram bytes read + written per unit, measured with ncu on smaller snapshots of the same
-# mixture (profiles/k_rebind_loop_workload2.md, profiles/k_density_f_workload2.md); traffic grows with
-# the units processed, so a full-size launch's traffic is taken as units times these figures
+# mixture (the first rebinding launch of a 1M snapshot; the density launch of a 4M one);
+# traffic grows with the units processed, so a full-size launch's traffic is taken as units
+# times these figures
 REBIND_TRAFFIC_PER_MEMBER = (642_154_240 + 417_524_992) / 662_193    # first launch, 1M snapshot: 1,600 B
 DENSITY_TRAFFIC_PER_POINT = (928_974_848 + 483_069_184) / 6_736_104  # 4M snapshot: 209.6 B
 # the catalogue of the benchmarked snapshot as the unmodified reference writes it
@@ -404,7 +405,7 @@ def run_gpu(args) -> None:
     roof = {"kernel": "k_rebind_loop (Hill-sphere rebinding, every clump's calls on the device; all launches of one snapshot)",
             "bound": "hbm", "achieved": rb_achieved, "peak": peak, "unit": "GB/s", "frac": rb_achieved / peak if rb_achieved else None,
             "peak_kind": f"{peak_kind} HBM copy bandwidth", "traffic": REBIND_TRAFFIC_PER_MEMBER * rb_members,
-            "traffic_note": "dram bytes read+written per member from one ncu capture (profiles/), times the members of the step's passes",
+            "traffic_note": "dram bytes read+written per member from one ncu capture (first launch, 1M snapshot), times the members of the step's passes",
             "bytes_per_unit": REBIND_BYTES_PER_MEMBER, "units": rb_members, "kernel_ms": rb_ms,
             "limited_by": "dependent FP64 update chains and exact ordered member sums, not bandwidth"}
     dens_avg = float(np.mean(dens_ms))
